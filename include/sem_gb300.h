@@ -1,0 +1,221 @@
+/*
+ * sem_gb300.h -- C ABI of the GB300 (sm_103a) spectral-element library.
+ *
+ * This is the drop-in boundary for arotem3/SchrodingerSEM's hot path: the
+ * matrix-free SEM operator apply, the element-interface gather-scatter and
+ * Dirichlet masking, and the MINRES / PCG iterations behind the Poisson,
+ * Helmholtz and Schroedinger (BDF2, SDIRK4 3-stage, SDIRK4 5-stage) solvers.
+ * Each entry point names the reference interface it replaces (file:line in
+ * the reference project).  The C++ layer in include/schro_gpu/ rebuilds the
+ * reference's template API (minres, pcg, solver_results, solver_opts, ...)
+ * on top of these calls.
+ *
+ * Conventions
+ *  - A "field" is E*N*N doubles (N = p+1), element-contiguous, each element a
+ *    column-major N x N block: value (i,j) of element e at e*N*N + j*N + i,
+ *    i the xi index, j the eta index.  This is the memory of the reference's
+ *    std::vector<arma::Mat<double>> laid end to end.
+ *  - Field pointers of the operator-level calls (sem_unmask ... sem_pcg_*)
+ *    are DEVICE pointers.  The driver-level calls (sem_poisson,
+ *    sem_helmholtz, sem_schrodinger_*) accept host or device pointers and
+ *    copy host data in and out themselves.
+ *  - Every call returns an int status (SEM_OK = 0).  Solver non-convergence
+ *    is not an error: it is reported in sem_solver_results.success or the
+ *    driver's *success flag, as the reference does.
+ *  - One context = one mesh + its device buffers, bound to one CUDA stream.
+ *    Calls on one context are not reentrant.  Operator-level calls are
+ *    asynchronous on that stream, except those that return a host scalar.
+ */
+#ifndef SEM_GB300_H
+#define SEM_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEM_GB300_VERSION 1
+
+/* status codes */
+enum sem_status {
+    SEM_OK = 0,
+    SEM_ERR_ARG = 1,          /* bad argument (null pointer, size, degree out of range) */
+    SEM_ERR_CUDA = 2,         /* a CUDA runtime call failed */
+    SEM_ERR_MESH = 3,         /* mesh topology invalid (bad corner id, not a quad mesh) */
+    SEM_ERR_IO = 4,           /* mesh folder could not be read */
+    SEM_ERR_DEVICE_WAIT = 5,  /* a device-side wait hit its time limit; results invalid */
+    SEM_ERR_UNSUPPORTED = 6,  /* request outside what this build supports */
+    SEM_ERR_NO_DEVICE = 7     /* no CUDA device visible */
+};
+
+/* context creation flags */
+#define SEM_FLAG_METRIC_CORRECTED 0x1u /* C(i,j) = (Y_xi[j]^2 + X_xi[j]^2)/J.  Without this
+                                          flag the reference's formula include/Quad.hpp:53
+                                          (Y_xi[i]^2) is reproduced, for parity. */
+
+/* options for sem_ctx_set_option */
+enum sem_option {
+    SEM_OPT_SOLVE_PRECISION = 1, /* SEM_PREC_FP64 (default) or SEM_PREC_MIXED */
+    SEM_OPT_INNER_TOL = 2,       /* relative tolerance of the FP32 inner solve (default 1e-4) */
+    SEM_OPT_STAGE_GUESS = 3,     /* SEM_GUESS_ZERO (reference), _EXTRAPOLATE, _LEARNED */
+    SEM_OPT_WAIT_TIMEOUT_MS = 4, /* limit of every device-side wait (default 2000 ms) */
+    SEM_OPT_MAX_REFINE = 5       /* cap on FP64 refinement sweeps in mixed mode (default 50) */
+};
+enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
+enum { SEM_GUESS_ZERO = 0, SEM_GUESS_EXTRAPOLATE = 1, SEM_GUESS_LEARNED = 2 };
+
+typedef struct sem_ctx sem_ctx;
+
+/* include/solver_base.hpp:6-12 (solver_results<double>) */
+typedef struct {
+    int success;
+    int n_iter;
+    double residual;
+} sem_solver_results;
+
+/* include/ode_base.hpp:6-13 (solver_opts<double>) */
+typedef struct {
+    int max_iter;
+    double tol;
+    double dt;
+    int verbose;
+} sem_solver_opts;
+
+typedef struct {
+    int p, N;
+    int n_elements, n_nodes, n_edges;
+    int n_interior_edges, n_boundary_edges, n_boundary_nodes;
+    long long n_local;      /* E*N*N */
+    long long dof;          /* include/openmp_impl/Mesh.hpp:84-87 */
+} sem_mesh_info;
+
+typedef struct {
+    long long krylov_iterations;    /* total MINRES/PCG iterations since creation */
+    long long fp64_applies;         /* operator applies done in FP64 */
+    long long fp32_applies;         /* operator applies done in FP32 */
+    int last_step_stages;           /* stages in the last time step */
+    int last_stage_iters[8];        /* Krylov iterations (inner, summed over sweeps) per stage */
+    int last_stage_sweeps[8];       /* FP64 refinement sweeps per stage (1 in FP64 mode) */
+    double last_error_estimate;     /* SDIRK4 5-stage embedded estimate (schrodinger.hpp:262-263) */
+    int steps_taken;                /* steps of the last driver call */
+} sem_stats;
+
+/* after each accepted step; nonzero return stops the time loop
+ * (include/openmp_impl/schrodinger.hpp:116-118).  psi_re/psi_im point to
+ * the caller's own buffers (host or device, as passed in), which already
+ * hold the state after the step. */
+typedef int (*sem_step_callback)(void* user, int step, const double* psi_re, const double* psi_im);
+
+/* ---------------------------------------------------------------- misc */
+int sem_version(void);
+const char* sem_status_string(int status);
+/* last error message of the calling thread ("" if none) */
+const char* sem_last_error(void);
+
+/* ---------------------------------------------------------------- mesh */
+
+/* load_mesh<Mesh>(p, folder) + Mesh::compute_metrics()
+ * (include/load_mesh.hpp:76-209, include/openmp_impl/Mesh.hpp:70-75) from
+ * in-memory arrays: coords = n_nodes (x,y) pairs, elements = n_elements x 4
+ * counter-clockwise corner ids.  1 <= p <= 16. */
+int sem_ctx_create(sem_ctx** ctx, int p, int n_nodes, const double* coords,
+                   int n_elements, const int* elements, unsigned flags);
+/* the same from the reference's mesh folder (info.txt, coordinates.txt,
+ * elements.txt; include/load_mesh.hpp:90-144) */
+int sem_ctx_load(sem_ctx** ctx, int p, const char* folder, unsigned flags);
+int sem_ctx_destroy(sem_ctx* ctx);
+int sem_ctx_get_info(const sem_ctx* ctx, sem_mesh_info* info);
+/* bind the context to a cudaStream_t (NULL = legacy default stream) */
+int sem_ctx_set_stream(sem_ctx* ctx, void* cuda_stream);
+int sem_ctx_set_option(sem_ctx* ctx, int option, double value);
+int sem_ctx_get_stats(const sem_ctx* ctx, sem_stats* stats);
+/* quad_rule (include/gauss_lobatto.hpp:27-32) and Mesh::D
+ * (include/load_mesh.hpp:83): x, w hold N values, D N*N column-major.
+ * Host pointers; any may be NULL. */
+int sem_ctx_get_quadrature(const sem_ctx* ctx, double* x, double* w, double* D);
+/* Quad::J, A, B, C of every element (include/Quad.hpp:17-20) as fields.
+ * Host pointers; any may be NULL. */
+int sem_ctx_get_metrics(const sem_ctx* ctx, double* J, double* A, double* B, double* C);
+/* Quad::from_local_coo (include/Quad.hpp:57-62) at every element-local node.
+ * Host pointers. */
+int sem_ctx_get_node_coords(const sem_ctx* ctx, double* x, double* y);
+
+/* ---------------------------------------------- gather-scatter (device) */
+
+/* schro_omp::unmask (include/openmp_impl/unmask.hpp:43-55), in place */
+int sem_unmask(sem_ctx* ctx, double* a);
+/* schro_omp::global_sum (include/openmp_impl/global_sum.hpp:65-77), in place */
+int sem_global_sum(sem_ctx* ctx, double* a);
+/* schro_omp::mask (include/openmp_impl/mask.hpp:16-28), in place */
+int sem_mask(sem_ctx* ctx, double* a);
+/* schro_omp::dot (include/openmp_impl/dot.hpp:11-61); result to host */
+int sem_dot(sem_ctx* ctx, const double* a, const double* b, double* result);
+/* out = a*x + b*y over n values (y may be NULL, then out = a*x): the
+ * element-wise algebra of the reference's expression templates
+ * (include/Op.hpp:9-37, include/openmp_impl/solution_wrapper.hpp:150-185) */
+int sem_vec_axpby(sem_ctx* ctx, long long n, double a, const double* x, double b,
+                  const double* y, double* out);
+
+/* ---------------------------------------------------- operators (device) */
+
+/* schro_omp::gproj (include/openmp_impl/galerkin.hpp:42-57) */
+int sem_gproj(sem_ctx* ctx, const double* u, double* out);
+/* galerkin_op of glaplace: the Poisson operator
+ * (include/openmp_impl/poisson.hpp:31-47, include/glaplace.hpp:16-28) */
+int sem_apply_laplace(sem_ctx* ctx, const double* u, double* out);
+/* Helmholtz operator (include/openmp_impl/helmholtz.hpp:32-52) */
+int sem_apply_helmholtz(sem_ctx* ctx, const double* c, const double* u, double* out);
+/* Schroedinger Res closure [M u + a L v ; a L u - M v], L = K + M_V
+ * (include/openmp_impl/schrodinger.hpp:344-366) */
+int sem_apply_schro_res(sem_ctx* ctx, const double* V, double alpha,
+                        const double* q_re, const double* q_im, double* out_re, double* out_im);
+/* Schroedinger f closure [-L v ; -L u] (include/openmp_impl/schrodinger.hpp:322-342) */
+int sem_apply_schro_f(sem_ctx* ctx, const double* V,
+                      const double* q_re, const double* q_im, double* out_re, double* out_im);
+/* FP32 storage and arithmetic variant of sem_apply_schro_res (the operator
+ * the FP32 inner solver applies; no reference counterpart in float) */
+int sem_apply_schro_res_f32(sem_ctx* ctx, const float* V, float alpha,
+                            const float* q_re, const float* q_im, float* out_re, float* out_im);
+
+/* --------------------------------------------- Krylov solvers (device) */
+
+/* minres (include/minres.hpp:19-107) on the Schroedinger Res operator with
+ * the identity preconditioner, as schrodinger.hpp:97,223,380 call it.
+ * x in/out; x_is_zero != 0 promises x == 0 on entry (skips A(x)). */
+int sem_minres_schro(sem_ctx* ctx, const double* V, double alpha,
+                     double* x_re, double* x_im, const double* b_re, const double* b_im,
+                     int maxit, double tol, int x_is_zero, sem_solver_results* res);
+/* minres on the Helmholtz operator (include/openmp_impl/helmholtz.hpp:59) */
+int sem_minres_helmholtz(sem_ctx* ctx, const double* c, double* x, const double* b,
+                         int maxit, double tol, int x_is_zero, sem_solver_results* res);
+/* pcg (include/pcg.hpp:59-97) on the Poisson operator
+ * (include/openmp_impl/poisson.hpp:54) */
+int sem_pcg_laplace(sem_ctx* ctx, double* x, const double* b,
+                    int max_iter, double tol, int x_is_zero, sem_solver_results* res);
+
+/* --------------------------------------------- drivers (host or device) */
+
+/* schro_omp::poisson (include/openmp_impl/poisson.hpp:17-59) */
+int sem_poisson(sem_ctx* ctx, double* u, const double* f, int max_iter, double tol,
+                sem_solver_results* res);
+/* schro_omp::helmholtz (include/openmp_impl/helmholtz.hpp:18-64) */
+int sem_helmholtz(sem_ctx* ctx, double* u, const double* c, const double* f,
+                  int max_iter, double tol, sem_solver_results* res);
+/* schro_omp::schrodinger_bdf2 (include/openmp_impl/schrodinger.hpp:22-128) */
+int sem_schrodinger_bdf2(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
+                         double T, const sem_solver_opts* opts,
+                         sem_step_callback cb, void* user, int* success);
+/* schro_omp::schrodinger_dirk4s5 (include/openmp_impl/schrodinger.hpp:138-285) */
+int sem_schrodinger_dirk4s5(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
+                            double T, const sem_solver_opts* opts,
+                            sem_step_callback cb, void* user, int* success);
+/* schro_omp::schrodinger_dirk4s3 (include/openmp_impl/schrodinger.hpp:294-423) */
+int sem_schrodinger_dirk4s3(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
+                            double T, const sem_solver_opts* opts,
+                            sem_step_callback cb, void* user, int* success);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SEM_GB300_H */

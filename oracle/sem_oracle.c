@@ -1,0 +1,1130 @@
+/*
+ * sem_oracle.c -- CPU restatement of arotem3/SchrodingerSEM's OpenMP path.
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the CUDA library, never part of
+ * it.  Every function follows the reference function cited beside it, in the
+ * same order of operations, on the same element-local data layout.  Where the
+ * reference leans on a third-party library the published algorithm is
+ * restated here:
+ *   - Armadillo small dense products -> plain loops, k ascending;
+ *   - Boost.Math legendre_p / legendre_p_prime -> three-term recurrences;
+ *   - LAPACK dsteqr (eigenvalues of a symmetric tridiagonal) -> Sturm-sequence
+ *     bisection; the two Newton steps that follow it in the reference make the
+ *     nodes independent of how the eigenvalues were found, to rounding.
+ * Parity is pinned against the reference's own known-answer tests (see
+ * sem_oracle.h).  Compiled with -ffp-contract=off so x86 and Arm hosts give
+ * the same bits.
+ */
+#include "sem_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+void or_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}
+
+int or_get_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+/* ------------------------------------------------------------------ a1 */
+
+/* Legendre polynomial by the three-term recurrence
+ * (k+1) P_{k+1} = (2k+1) x P_k - k P_{k-1}. */
+double or_legendre_p(int n, double x)
+{
+    if (n == 0) return 1.0;
+    double p0 = 1.0, p1 = x;
+    for (int k = 1; k < n; ++k) {
+        double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+/* P'_{k+1} = P'_{k-1} + (2k+1) P_k, valid on the closed interval. */
+double or_legendre_p_prime(int n, double x)
+{
+    if (n == 0) return 0.0;
+    double dm1 = 0.0, d0 = 1.0; /* P'_0, P'_1 */
+    double pk = x;              /* P_1 */
+    double pkm1 = 1.0;          /* P_0 */
+    for (int k = 1; k < n; ++k) {
+        double d1 = dm1 + (2.0 * k + 1.0) * pk;
+        double pk1 = ((2.0 * k + 1.0) * x * pk - k * pkm1) / (k + 1.0);
+        dm1 = d0;
+        d0 = d1;
+        pkm1 = pk;
+        pk = pk1;
+    }
+    return d0;
+}
+
+/* number of eigenvalues of the symmetric tridiagonal (diag d, offdiag e)
+ * strictly below s: Sturm sequence count of negative pivots. */
+static int sturm_count(int n, const double* d, const double* e, double s)
+{
+    int cnt = 0;
+    double q = d[0] - s;
+    if (q < 0) ++cnt;
+    for (int i = 1; i < n; ++i) {
+        if (q == 0.0) q = DBL_EPSILON * 1e-3;
+        q = (d[i] - s) - e[i - 1] * e[i - 1] / q;
+        if (q < 0) ++cnt;
+    }
+    return cnt;
+}
+
+/* eigenvalues ascending, by bisection on [-1, 1] (all off-diagonals of the
+ * Jacobi matrix used below are < 1/2, so Gershgorin bounds them by 1). */
+static int tridiag_eigvals(int n, const double* d, const double* e, double* lam)
+{
+    for (int k = 0; k < n; ++k) {
+        double lo = -1.0, hi = 1.0;
+        for (int it = 0; it < 200; ++it) {
+            double mid = 0.5 * (lo + hi);
+            if (mid <= lo || mid >= hi) break;
+            if (sturm_count(n, d, e, mid) > k) hi = mid; else lo = mid;
+        }
+        lam[k] = 0.5 * (lo + hi);
+    }
+    return 0;
+}
+
+/* include/gauss_lobatto.hpp:43-126 */
+int or_gauss_lobatto(int n, double* xo, double* wo)
+{
+    if (n < 1) return -1;
+    /* the reference's cached rules for n <= 8, to the digits it states
+     * (include/gauss_lobatto.hpp:49-58); parity depends on these values */
+    static const double t1[] = {-1, 1};
+    static const double t2[] = {-1, 0, 1};
+    static const double t3[] = {-1, -0.447213595499958, 0.447213595499958, 1};
+    static const double t4[] = {-1, -0.654653670707977, 0, 0.654653670707977, 1};
+    static const double t5[] = {-1, -0.765055323929465, -0.285231516480645, 0.285231516480645,
+                                0.765055323929465, 1};
+    static const double t6[] = {-1, -0.830223896278567, -0.468848793470714, 0.0, 0.468848793470714,
+                                0.830223896278567, 1};
+    static const double t7[] = {-1, -0.871740148509607, -0.591700181433142, -0.209299217902479,
+                                0.2092992179024789, 0.591700181433142, 0.871740148509607, 1};
+    static const double t8[] = {-1, -0.899757995411460, -0.677186279510738, -0.363117463826178, 0,
+                                0.363117463826178, 0.677186279510738, 0.899757995411460, 1};
+    static const double* tab[] = {0, t1, t2, t3, t4, t5, t6, t7, t8};
+    if (n <= 8) {
+        memcpy(xo, tab[n], sizeof(double) * (n + 1));
+    } else {
+        /* Golub-Welsch: interior nodes are the eigenvalues of the Jacobi
+         * matrix of P^{(1,1)}_{n-1} (:65-92) */
+        int NN = n - 1;
+        double* D = (double*)calloc(NN, sizeof(double));
+        double* E = (double*)calloc(NN, sizeof(double));
+        double* lam = (double*)calloc(NN, sizeof(double));
+        for (int i = 0; i < n - 2; ++i) {
+            double ii = i + 1;
+            E[i] = sqrt(ii * (ii + 2) / ((2 * ii + 3) * (2 * ii + 1)));
+        }
+        tridiag_eigvals(NN, D, E, lam);
+        int h = NN / 2;
+        double* xs = (double*)calloc(n + 1, sizeof(double));
+        for (int i = 0; i < h; ++i) {
+            double z = lam[i];
+            /* two Newton steps on P_{n+1} - P_{n-1} (:94-101) */
+            for (int it = 0; it < 2; ++it) {
+                double q = or_legendre_p(n + 1, z) - or_legendre_p(n - 1, z);
+                double dq = or_legendre_p_prime(n + 1, z) - or_legendre_p_prime(n - 1, z);
+                z -= q / dq;
+            }
+            xs[i] = z;
+        }
+        int cnt = h;
+        if (n % 2 == 0) xs[cnt++] = 0; /* :103-104 */
+        for (int i = h - 1; i >= 0; --i) xs[cnt++] = -xs[i]; /* :106-108 */
+        xo[0] = -1;
+        for (int i = 0; i < cnt; ++i) xo[i + 1] = xs[i];
+        xo[n] = 1;
+        free(D);
+        free(E);
+        free(lam);
+        free(xs);
+    }
+    /* weights (:116-123) */
+    wo[0] = 2.0 / (n * (n + 1));
+    wo[n] = wo[0];
+    for (int i = 0; i < n / 2 + 1; ++i) {
+        double pn = or_legendre_p(n, xo[i]);
+        wo[i] = 2.0 / (n * (n + 1) * (pn * pn));
+        wo[n - i] = wo[i];
+    }
+    return 0;
+}
+
+/* ------------------------------------------------------------------ a2 */
+
+/* include/derivative_matrix.hpp:12-38 (barycentric form) */
+void or_derivative_matrix(int n, const double* x, double* D)
+{
+    double* w = (double*)malloc(sizeof(double) * n);
+    for (int i = 0; i < n; ++i) {
+        w[i] = 1.0;
+        for (int j = 0; j < n; ++j)
+            if (i != j) w[i] *= x[i] - x[j];
+        w[i] = 1 / w[i];
+    }
+    memset(D, 0, sizeof(double) * n * n);
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            if (j != i) {
+                D[i + j * n] = (w[j] / w[i]) / (x[i] - x[j]);
+                D[i + i * n] -= D[i + j * n];
+            }
+    free(w);
+}
+
+/* ------------------------------------------------------------------ a17 */
+
+typedef struct { long key; int idx; } hslot;
+
+static long pair_key(int a, int b, int n_nodes)
+{
+    int lo = a < b ? a : b, hi = a < b ? b : a;
+    return (long)lo * (long)n_nodes + hi;
+}
+
+or_mesh* or_mesh_create(int p, int n_nodes, const double* coords, int n_el, const int* elements)
+{
+    if (p < 1 || n_nodes <= 0 || n_el <= 0) return NULL;
+    or_mesh* m = (or_mesh*)calloc(1, sizeof(or_mesh));
+    m->p = p;
+    m->N = p + 1;
+    m->n_nodes = n_nodes;
+    m->n_el = n_el;
+    int N = m->N;
+    m->x = (double*)malloc(sizeof(double) * N);
+    m->w = (double*)malloc(sizeof(double) * N);
+    m->D = (double*)malloc(sizeof(double) * N * N);
+    or_gauss_lobatto(p, m->x, m->w);        /* Mesh(int p), openmp_impl/Mesh.hpp:39-42 */
+    or_derivative_matrix(N, m->x, m->D);    /* load_mesh.hpp:83 */
+
+    const int cmap1[] = {0, N - 1, N - 1, 0}; /* load_mesh.hpp:85-88 */
+    const int cmap2[] = {0, 0, N - 1, N - 1};
+    const int emap1[] = {0, 1, 3, 0};
+    const int emap2[] = {1, 2, 2, 3};
+
+    m->node_x = (double*)malloc(sizeof(double) * n_nodes);
+    m->node_y = (double*)malloc(sizeof(double) * n_nodes);
+    m->node_type = (int*)calloc(n_nodes, sizeof(int));
+    for (int k = 0; k < n_nodes; ++k) {
+        m->node_x[k] = coords[2 * k];
+        m->node_y[k] = coords[2 * k + 1];
+    }
+    m->xs = (double*)malloc(sizeof(double) * 4 * n_el);
+    m->ys = (double*)malloc(sizeof(double) * 4 * n_el);
+    m->corner_ids = (int*)malloc(sizeof(int) * 4 * n_el);
+    /* connected_elements lists in element order (load_mesh.hpp:123-143) */
+    m->node_ptr = (int*)calloc(n_nodes + 1, sizeof(int));
+    for (int e = 0; e < n_el; ++e)
+        for (int i = 0; i < 4; ++i) {
+            int c = elements[4 * e + i];
+            if (c < 0 || c >= n_nodes) { or_mesh_free(m); return NULL; }
+            m->node_ptr[c + 1]++;
+        }
+    for (int k = 0; k < n_nodes; ++k) m->node_ptr[k + 1] += m->node_ptr[k];
+    int* fill = (int*)calloc(n_nodes, sizeof(int));
+    m->node_el = (int*)malloc(sizeof(int) * 4 * n_el);
+    m->node_i = (int*)malloc(sizeof(int) * 4 * n_el);
+    m->node_j = (int*)malloc(sizeof(int) * 4 * n_el);
+    for (int e = 0; e < n_el; ++e)
+        for (int i = 0; i < 4; ++i) {
+            int c = elements[4 * e + i];
+            int pos = m->node_ptr[c] + fill[c]++;
+            m->node_el[pos] = e;
+            m->node_i[pos] = cmap1[i];
+            m->node_j[pos] = cmap2[i];
+            m->corner_ids[4 * e + i] = c;
+            m->xs[4 * e + i] = m->node_x[c];
+            m->ys[4 * e + i] = m->node_y[c];
+        }
+    free(fill);
+
+    /* unique edges keyed by the sorted corner pair (load_mesh.hpp:146-176) */
+    int cap = 16;
+    while (cap < 8 * n_el) cap <<= 1;
+    hslot* tab = (hslot*)malloc(sizeof(hslot) * cap);
+    for (int k = 0; k < cap; ++k) tab[k].key = -1;
+    int max_edges = 4 * n_el;
+    m->edge_type = (int*)malloc(sizeof(int) * max_edges);
+    m->edge_el = (int*)malloc(sizeof(int) * 2 * max_edges);
+    m->edge_side = (int*)malloc(sizeof(int) * 2 * max_edges);
+    m->edge_start = (int*)malloc(sizeof(int) * max_edges);
+    m->edge_delta = (int*)malloc(sizeof(int) * max_edges);
+    int ne = 0;
+    for (int e = 0; e < n_el; ++e)
+        for (int i = 0; i < 4; ++i) {
+            int start = m->corner_ids[4 * e + emap1[i]];
+            int end = m->corner_ids[4 * e + emap2[i]];
+            long key = pair_key(start, end, n_nodes);
+            unsigned long hsh = (unsigned long)key * 0x9E3779B97F4A7C15UL;
+            int slot = (int)(hsh >> 20) & (cap - 1);
+            while (tab[slot].key != -1 && tab[slot].key != key) slot = (slot + 1) & (cap - 1);
+            if (tab[slot].key == key) {
+                int ed = tab[slot].idx;
+                int e0 = m->edge_el[2 * ed];
+                int s0 = m->edge_side[2 * ed];
+                int n1 = m->corner_ids[4 * e0 + emap1[s0 - 1]];
+                m->edge_el[2 * ed + 1] = e;
+                m->edge_type[ed] = OR_INTERIOR;
+                m->edge_side[2 * ed + 1] = (start == n1) ? (i + 1) : -(i + 1);
+            } else {
+                tab[slot].key = key;
+                tab[slot].idx = ne;
+                m->edge_type[ne] = OR_BOUNDARY; /* Edge(int el, int side), Edge.hpp:19-26 */
+                m->edge_el[2 * ne] = e;
+                m->edge_el[2 * ne + 1] = -1;
+                m->edge_side[2 * ne] = i + 1;
+                m->edge_side[2 * ne + 1] = 0;
+                m->edge_start[ne] = 0;
+                m->edge_delta[ne] = 0;
+                ++ne;
+            }
+        }
+    free(tab);
+    m->n_edges = ne;
+    /* boundary flags and orientation (load_mesh.hpp:181-206) */
+    for (int ed = 0; ed < ne; ++ed) {
+        if (m->edge_type[ed] == OR_BOUNDARY) {
+            int e = m->edge_el[2 * ed];
+            int s = m->edge_side[2 * ed];
+            m->node_type[m->corner_ids[4 * e + emap1[s - 1]]] = OR_BOUNDARY;
+            m->node_type[m->corner_ids[4 * e + emap2[s - 1]]] = OR_BOUNDARY;
+        } else if (m->edge_side[2 * ed + 1] > 0) {
+            m->edge_start[ed] = 1;
+            m->edge_delta[ed] = 1;
+        } else {
+            m->edge_start[ed] = N - 2;
+            m->edge_delta[ed] = -1;
+        }
+    }
+    size_t nn = (size_t)n_el * N * N;
+    m->J = (double*)malloc(sizeof(double) * nn);
+    m->A = (double*)malloc(sizeof(double) * nn);
+    m->B = (double*)malloc(sizeof(double) * nn);
+    m->C = (double*)malloc(sizeof(double) * nn);
+    return m;
+}
+
+or_mesh* or_mesh_load(int p, const char* folder)
+{
+    char path[4096];
+    snprintf(path, sizeof path, "%s/info.txt", folder);
+    FILE* f = fopen(path, "r");
+    if (!f) return NULL;
+    int n_nodes = 0, n_el = 0;
+    if (fscanf(f, "%d %d", &n_nodes, &n_el) != 2) { fclose(f); return NULL; }
+    fclose(f);
+    double* coo = (double*)malloc(sizeof(double) * 2 * n_nodes);
+    int* el = (int*)malloc(sizeof(int) * 4 * n_el);
+    snprintf(path, sizeof path, "%s/coordinates.txt", folder);
+    f = fopen(path, "r");
+    if (!f) { free(coo); free(el); return NULL; }
+    for (int k = 0; k < 2 * n_nodes; ++k)
+        if (fscanf(f, "%lf", &coo[k]) != 1) { fclose(f); free(coo); free(el); return NULL; }
+    fclose(f);
+    snprintf(path, sizeof path, "%s/elements.txt", folder);
+    f = fopen(path, "r");
+    if (!f) { free(coo); free(el); return NULL; }
+    for (int k = 0; k < 4 * n_el; ++k)
+        if (fscanf(f, "%d", &el[k]) != 1) { fclose(f); free(coo); free(el); return NULL; }
+    fclose(f);
+    or_mesh* m = or_mesh_create(p, n_nodes, coo, n_el, el);
+    free(coo);
+    free(el);
+    return m;
+}
+
+/* include/Quad.hpp:27-55 over all elements (openmp_impl/Mesh.hpp:70-75) */
+void or_mesh_compute_metrics(or_mesh* m, int ref_compat)
+{
+    const int N = m->N;
+    const double* z = m->x;
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) {
+        const double* xs = m->xs + 4 * e;
+        const double* ys = m->ys + 4 * e;
+        double Xxi[32], Yxi[32], Xeta[32], Yeta[32];
+        for (int i = 0; i < N; ++i) {
+            Xxi[i] = 0.25 * ((1 - z[i]) * (xs[1] - xs[0]) + (1 + z[i]) * (xs[2] - xs[3]));
+            Yxi[i] = 0.25 * ((1 - z[i]) * (ys[1] - ys[0]) + (1 + z[i]) * (ys[2] - ys[3]));
+            Xeta[i] = 0.25 * ((1 - z[i]) * (xs[3] - xs[0]) + (1 + z[i]) * (xs[2] - xs[1]));
+            Yeta[i] = 0.25 * ((1 - z[i]) * (ys[3] - ys[0]) + (1 + z[i]) * (ys[2] - ys[1]));
+        }
+        size_t off = (size_t)e * N * N;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                size_t k = off + i + (size_t)j * N;
+                double Jij = Xxi[j] * Yeta[i] - Xeta[i] * Yxi[j];
+                m->J[k] = Jij;
+                m->A[k] = (Yeta[i] * Yeta[i] + Xeta[i] * Xeta[i]) / Jij;
+                m->B[k] = (Yeta[i] * Yxi[j] + Xeta[i] * Xxi[j]) / Jij;
+                if (ref_compat)
+                    m->C[k] = (Yxi[i] * Yxi[i] + Xxi[j] * Xxi[j]) / Jij; /* Quad.hpp:53 as written */
+                else
+                    m->C[k] = (Yxi[j] * Yxi[j] + Xxi[j] * Xxi[j]) / Jij;
+            }
+    }
+}
+
+void or_mesh_free(or_mesh* m)
+{
+    if (!m) return;
+    free(m->x); free(m->w); free(m->D);
+    free(m->xs); free(m->ys); free(m->corner_ids);
+    free(m->edge_type); free(m->edge_el); free(m->edge_side);
+    free(m->edge_start); free(m->edge_delta);
+    free(m->node_type); free(m->node_x); free(m->node_y);
+    free(m->node_ptr); free(m->node_el); free(m->node_i); free(m->node_j);
+    free(m->J); free(m->A); free(m->B); free(m->C);
+    free(m);
+}
+
+/* include/openmp_impl/Mesh.hpp:84-87 */
+int or_mesh_dof(const or_mesh* m)
+{
+    return m->n_nodes + m->n_edges * (m->N - 2) + m->n_el * (m->N - 2) * (m->N - 2);
+}
+
+/* include/Quad.hpp:57-62 */
+void or_mesh_node_coords(const or_mesh* m, double* X, double* Y)
+{
+    const int N = m->N;
+    for (int e = 0; e < m->n_el; ++e) {
+        const double* xs = m->xs + 4 * e;
+        const double* ys = m->ys + 4 * e;
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                double xi = m->x[i], eta = m->x[j];
+                size_t k = (size_t)e * N * N + i + (size_t)j * N;
+                X[k] = 0.25 * (xs[0] * (1 - xi) * (1 - eta) + xs[1] * (1 + xi) * (1 - eta) +
+                               xs[2] * (1 + xi) * (1 + eta) + xs[3] * (1 - xi) * (1 + eta));
+                Y[k] = 0.25 * (ys[0] * (1 - xi) * (1 - eta) + ys[1] * (1 + xi) * (1 - eta) +
+                               ys[2] * (1 + xi) * (1 + eta) + ys[3] * (1 - xi) * (1 + eta));
+            }
+    }
+}
+
+/* ------------------------------------------------------------------ a8-a11 */
+
+#define AT(a, e, i, j) (a)[(size_t)(e) * NN + (i) + (size_t)(j) * N]
+
+/* Mesh::smap, openmp_impl/Mesh.hpp:78-82 */
+static inline int smap(int N, int side)
+{
+    const int s[] = {0, N - 1, N - 1, 0};
+    return s[side - 1];
+}
+
+/* get_edge_values.hpp:7-21: out[k], k = 1..N-2 */
+static void get_edge(const or_mesh* m, const double* a, int e, int s, double* out)
+{
+    const int N = m->N, NN = N * N;
+    out[0] = out[N - 1] = 0;
+    if (s == 2 || s == 4) {
+        int i = smap(N, s);
+        for (int j = 1; j < N - 1; ++j) out[j] = AT(a, e, i, j);
+    } else {
+        int j = smap(N, s);
+        for (int i = 1; i < N - 1; ++i) out[i] = AT(a, e, i, j);
+    }
+}
+
+/* set_edge_values.hpp:9-30 */
+static void set_edge(const or_mesh* m, double* a, int ed, const double* vals, int e, int s)
+{
+    const int N = m->N, NN = N * N;
+    if (s == 2 || s == 4) {
+        int i = smap(N, s);
+        int j = m->edge_start[ed];
+        for (int k = 1; k < N - 1; ++k) {
+            AT(a, e, i, j) = vals[k];
+            j += m->edge_delta[ed];
+        }
+    } else {
+        int j = smap(N, s);
+        int i = m->edge_start[ed];
+        for (int k = 1; k < N - 1; ++k) {
+            AT(a, e, i, j) = vals[k];
+            i += m->edge_delta[ed];
+        }
+    }
+}
+
+/* openmp_impl/unmask.hpp:12-55 */
+void or_unmask(const or_mesh* m, double* a)
+{
+    const int N = m->N, NN = N * N;
+    #pragma omp parallel for schedule(static)
+    for (int ed = 0; ed < m->n_edges; ++ed) {
+        if (m->edge_type[ed] == OR_BOUNDARY) continue;
+        double vals[32];
+        get_edge(m, a, m->edge_el[2 * ed], m->edge_side[2 * ed], vals);
+        set_edge(m, a, ed, vals, m->edge_el[2 * ed + 1], abs(m->edge_side[2 * ed + 1]));
+    }
+    #pragma omp parallel for schedule(static)
+    for (int c = 0; c < m->n_nodes; ++c) {
+        if (m->node_type[c] == OR_BOUNDARY) continue;
+        int p0 = m->node_ptr[c], p1 = m->node_ptr[c + 1];
+        if (p1 <= p0) continue;
+        double cval = AT(a, m->node_el[p0], m->node_i[p0], m->node_j[p0]);
+        for (int q = p0 + 1; q < p1; ++q) AT(a, m->node_el[q], m->node_i[q], m->node_j[q]) = cval;
+    }
+}
+
+/* openmp_impl/global_sum.hpp:13-77 */
+void or_global_sum(const or_mesh* m, double* a)
+{
+    const int N = m->N, NN = N * N;
+    #pragma omp parallel for schedule(static)
+    for (int ed = 0; ed < m->n_edges; ++ed) {
+        if (m->edge_type[ed] == OR_BOUNDARY) continue;
+        double ev[2][32];
+        for (int k = 0; k < 2; ++k)
+            get_edge(m, a, m->edge_el[2 * ed + k], abs(m->edge_side[2 * ed + k]), ev[k]);
+        int n = m->edge_start[ed], dn = m->edge_delta[ed];
+        for (int j = 1; j < N - 1; ++j) {
+            double s = ev[0][j] + ev[1][n];
+            ev[0][j] = s;
+            ev[1][n] = s;
+            n += dn;
+        }
+        for (int k = 0; k < 2; ++k) {
+            int e = m->edge_el[2 * ed + k];
+            int s = abs(m->edge_side[2 * ed + k]);
+            if (s == 2 || s == 4) {
+                int i = smap(N, s);
+                for (int j = 1; j < N - 1; ++j) AT(a, e, i, j) = ev[k][j];
+            } else {
+                int j = smap(N, s);
+                for (int i = 1; i < N - 1; ++i) AT(a, e, i, j) = ev[k][i];
+            }
+        }
+    }
+    #pragma omp parallel for schedule(static)
+    for (int c = 0; c < m->n_nodes; ++c) {
+        if (m->node_type[c] == OR_BOUNDARY) continue;
+        double csum = 0;
+        for (int q = m->node_ptr[c]; q < m->node_ptr[c + 1]; ++q)
+            csum += AT(a, m->node_el[q], m->node_i[q], m->node_j[q]);
+        for (int q = m->node_ptr[c]; q < m->node_ptr[c + 1]; ++q)
+            AT(a, m->node_el[q], m->node_i[q], m->node_j[q]) = csum;
+    }
+}
+
+/* openmp_impl/mask.hpp:16-28, mask_side.hpp:12-52, mask_node.hpp:8-22 */
+void or_mask(const or_mesh* m, double* a)
+{
+    const int N = m->N, NN = N * N;
+    #pragma omp parallel for schedule(static)
+    for (int ed = 0; ed < m->n_edges; ++ed) {
+        int e, s;
+        if (m->edge_type[ed] == OR_BOUNDARY) {
+            e = m->edge_el[2 * ed];
+            s = m->edge_side[2 * ed];
+        } else {
+            e = m->edge_el[2 * ed + 1];
+            s = abs(m->edge_side[2 * ed + 1]);
+        }
+        if (s == 2 || s == 4) {
+            int i = smap(N, s);
+            for (int j = 1; j < N - 1; ++j) AT(a, e, i, j) = 0;
+        } else {
+            int j = smap(N, s);
+            for (int i = 1; i < N - 1; ++i) AT(a, e, i, j) = 0;
+        }
+    }
+    #pragma omp parallel for schedule(static)
+    for (int c = 0; c < m->n_nodes; ++c) {
+        int q = m->node_ptr[c];
+        if (m->node_type[c] != OR_BOUNDARY) ++q;
+        for (; q < m->node_ptr[c + 1]; ++q) AT(a, m->node_el[q], m->node_i[q], m->node_j[q]) = 0.0;
+    }
+}
+
+/* openmp_impl/dot.hpp:11-61 */
+double or_dot(const or_mesh* m, const double* a, const double* b)
+{
+    const int N = m->N, NN = N * N;
+    double p_int = 0, p_edges = 0, p_corners = 0;
+    #pragma omp parallel for reduction(+ : p_int) schedule(static)
+    for (int e = 0; e < m->n_el; ++e) {
+        double s = 0;
+        for (int j = 1; j < N - 1; ++j)
+            for (int i = 1; i < N - 1; ++i) s += AT(a, e, i, j) * AT(b, e, i, j);
+        p_int += s;
+    }
+    #pragma omp parallel for reduction(+ : p_edges) schedule(static)
+    for (int ed = 0; ed < m->n_edges; ++ed) {
+        int e = m->edge_el[2 * ed];
+        int s = abs(m->edge_side[2 * ed]);
+        double pe = 0;
+        if (s == 2 || s == 4) {
+            int i = smap(N, s);
+            for (int j = 1; j < N - 1; ++j) pe += AT(a, e, i, j) * AT(b, e, i, j);
+        } else {
+            int j = smap(N, s);
+            for (int i = 1; i < N - 1; ++i) pe += AT(a, e, i, j) * AT(b, e, i, j);
+        }
+        p_edges += pe;
+    }
+    #pragma omp parallel for reduction(+ : p_corners) schedule(static)
+    for (int c = 0; c < m->n_nodes; ++c) {
+        int q = m->node_ptr[c];
+        if (q >= m->node_ptr[c + 1]) continue;
+        p_corners += AT(a, m->node_el[q], m->node_i[q], m->node_j[q]) *
+                     AT(b, m->node_el[q], m->node_i[q], m->node_j[q]);
+    }
+    return p_int + p_edges + p_corners;
+}
+
+/* ------------------------------------------------------------------ a4-a7 */
+
+/* include/glaplace.hpp:16-28 */
+void or_glaplace(const or_mesh* m, int e, const double* u, double* out)
+{
+    const int N = m->N, NN = N * N;
+    const double* D = m->D;
+    const double* w = m->w;
+    const double* A = m->A + (size_t)e * NN;
+    const double* B = m->B + (size_t)e * NN;
+    const double* C = m->C + (size_t)e * NN;
+    double uxi[32 * 32], ueta[32 * 32], T1[32 * 32], T2[32 * 32];
+#define M2(a, i, j) (a)[(i) + (j) * N]
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double s = 0;
+            for (int k = 0; k < N; ++k) s += M2(D, i, k) * M2(u, k, j); /* D * u */
+            M2(uxi, i, j) = s;
+            double t = 0;
+            for (int k = 0; k < N; ++k) t += M2(u, i, k) * M2(D, j, k); /* u * D.t() */
+            M2(ueta, i, j) = t;
+        }
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            M2(T1, i, j) = w[i] * (M2(A, i, j) * M2(uxi, i, j) - M2(B, i, j) * M2(ueta, i, j));
+            M2(T2, i, j) = (M2(C, i, j) * M2(ueta, i, j) - M2(B, i, j) * M2(uxi, i, j)) * w[j];
+        }
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double F = 0, G = 0;
+            for (int k = 0; k < N; ++k) F += M2(D, k, i) * M2(T1, k, j); /* D.t() * T1 */
+            for (int k = 0; k < N; ++k) G += M2(T2, i, k) * M2(D, k, j); /* T2 * D */
+            M2(out, i, j) = F * w[j] + w[i] * G;
+        }
+#undef M2
+}
+
+/* (diagmat(w) * (u % c) * diagmat(w)) % J for one element; c == NULL -> 1 */
+static void mass_term(const or_mesh* m, int e, const double* u, const double* c, double* out)
+{
+    const int N = m->N, NN = N * N;
+    const double* J = m->J + (size_t)e * NN;
+    for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+            double v = u[i + j * N];
+            if (c) v = v * c[i + j * N];
+            out[i + j * N] = ((m->w[i] * v) * m->w[j]) * J[i + j * N];
+        }
+}
+
+/* openmp_impl/galerkin.hpp:42-57 */
+void or_gproj(const or_mesh* m, const double* u, double* out)
+{
+    const int N = m->N, NN = N * N;
+    size_t n = (size_t)m->n_el * NN;
+    double* t = (double*)malloc(sizeof(double) * n);
+    memcpy(t, u, sizeof(double) * n);
+    or_unmask(m, t);
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) mass_term(m, e, t + (size_t)e * NN, NULL, out + (size_t)e * NN);
+    free(t);
+    or_global_sum(m, out);
+    or_mask(m, out);
+}
+
+/* galerkin_op(glaplace), openmp_impl/galerkin.hpp:24-35 + poisson.hpp:31-47 */
+void or_apply_laplace(const or_mesh* m, const double* u, double* out)
+{
+    const int NN = m->N * m->N;
+    size_t n = (size_t)m->n_el * NN;
+    double* t = (double*)malloc(sizeof(double) * n);
+    memcpy(t, u, sizeof(double) * n);
+    or_unmask(m, t);
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) or_glaplace(m, e, t + (size_t)e * NN, out + (size_t)e * NN);
+    free(t);
+    or_global_sum(m, out);
+    or_mask(m, out);
+}
+
+/* openmp_impl/helmholtz.hpp:32-52 */
+void or_apply_helmholtz(const or_mesh* m, const double* c, const double* u, double* out)
+{
+    const int NN = m->N * m->N;
+    size_t n = (size_t)m->n_el * NN;
+    double* t = (double*)malloc(sizeof(double) * n);
+    memcpy(t, u, sizeof(double) * n);
+    or_unmask(m, t);
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) {
+        double cuv[32 * 32], lap[32 * 32];
+        size_t off = (size_t)e * NN;
+        mass_term(m, e, t + off, c + off, cuv);
+        or_glaplace(m, e, t + off, lap);
+        for (int k = 0; k < NN; ++k) out[off + k] = cuv[k] + lap[k];
+    }
+    free(t);
+    or_global_sum(m, out);
+    or_mask(m, out);
+}
+
+/* L closure, schrodinger.hpp:314-320: glaplace(u) + (W (u%V) W) % J */
+static void schro_L(const or_mesh* m, int e, const double* u, const double* V, double* out)
+{
+    const int NN = m->N * m->N;
+    double pv[32 * 32];
+    size_t off = (size_t)e * NN;
+    mass_term(m, e, u, V + off, pv);
+    or_glaplace(m, e, u, out);
+    for (int k = 0; k < NN; ++k) out[k] = out[k] + pv[k];
+}
+
+/* Res closure, schrodinger.hpp:344-366 */
+void or_schro_res(const or_mesh* m, const double* V, double alpha,
+                  const double* q_re, const double* q_im, double* y_re, double* y_im)
+{
+    const int NN = m->N * m->N;
+    size_t n = (size_t)m->n_el * NN;
+    double* u = (double*)malloc(sizeof(double) * n);
+    double* v = (double*)malloc(sizeof(double) * n);
+    memcpy(u, q_re, sizeof(double) * n);
+    memcpy(v, q_im, sizeof(double) * n);
+    or_unmask(m, u);
+    or_unmask(m, v);
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) {
+        double pu[32 * 32], pv[32 * 32], Lu[32 * 32], Lv[32 * 32];
+        size_t off = (size_t)e * NN;
+        mass_term(m, e, u + off, NULL, pu);
+        mass_term(m, e, v + off, NULL, pv);
+        schro_L(m, e, v + off, V, Lv);
+        schro_L(m, e, u + off, V, Lu);
+        for (int k = 0; k < NN; ++k) {
+            y_re[off + k] = pu[k] + alpha * Lv[k];
+            y_im[off + k] = alpha * Lu[k] - pv[k];
+        }
+    }
+    free(u);
+    free(v);
+    or_global_sum(m, y_re);
+    or_global_sum(m, y_im);
+    or_mask(m, y_re);
+    or_mask(m, y_im);
+}
+
+/* f closure, schrodinger.hpp:322-342 */
+void or_schro_f(const or_mesh* m, const double* V,
+                const double* q_re, const double* q_im, double* y_re, double* y_im)
+{
+    const int NN = m->N * m->N;
+    size_t n = (size_t)m->n_el * NN;
+    double* u = (double*)malloc(sizeof(double) * n);
+    double* v = (double*)malloc(sizeof(double) * n);
+    memcpy(u, q_re, sizeof(double) * n);
+    memcpy(v, q_im, sizeof(double) * n);
+    or_unmask(m, u);
+    or_unmask(m, v);
+    #pragma omp parallel for schedule(static)
+    for (int e = 0; e < m->n_el; ++e) {
+        double Lu[32 * 32], Lv[32 * 32];
+        size_t off = (size_t)e * NN;
+        schro_L(m, e, v + off, V, Lv);
+        schro_L(m, e, u + off, V, Lu);
+        for (int k = 0; k < NN; ++k) {
+            y_re[off + k] = -Lv[k];
+            y_im[off + k] = -Lu[k];
+        }
+    }
+    free(u);
+    free(v);
+    or_global_sum(m, y_re);
+    or_global_sum(m, y_im);
+    or_mask(m, y_re);
+    or_mask(m, y_im);
+}
+
+/* ------------------------------------------------------------------ a13, a14 */
+
+static double* vnew(long n) { return (double*)calloc((size_t)n, sizeof(double)); }
+
+/* include/minres.hpp:19-107 (identity preconditioner, as every caller uses) */
+or_results or_minres(double* x, or_linop A, void* actx, const double* b, or_dotfn dot, void* dctx,
+                     long n, int maxit, double tol)
+{
+    int success = 0;
+    double* r1 = vnew(n);
+    double* r2 = vnew(n);
+    double* y = vnew(n);
+    double* v = vnew(n);
+    double* w = vnew(n);
+    double* w1 = vnew(n);
+    double* w2 = vnew(n);
+    A(actx, x, y);
+    #pragma omp parallel for schedule(static)
+    for (long k = 0; k < n; ++k) r1[k] = b[k] - y[k];         /* r1 = b - A(x) */
+    memcpy(y, r1, sizeof(double) * n);                         /* y = precond(r1) */
+    memcpy(r2, r1, sizeof(double) * n);                        /* r2 = r1 */
+    double b_norm = sqrt(dot(dctx, r1, r1));
+    double machine_epsilon = DBL_EPSILON;
+    double beta1 = sqrt(dot(dctx, y, r1));
+    double beta = beta1, beta_old = 0, tnorm = 0, dbar = 0, eps = 0, eps_old = 0, phibar = beta1,
+           cs = -1, sn = 0;
+    (void)tnorm;
+    int i;
+    for (i = 1; i <= maxit; ++i) {
+        double s = 1.0 / beta;
+        #pragma omp parallel for schedule(static)
+        for (long k = 0; k < n; ++k) v[k] = s * y[k];
+        A(actx, v, y);
+        if (i >= 2) {
+            double c = beta / beta_old;
+            #pragma omp parallel for schedule(static)
+            for (long k = 0; k < n; ++k) y[k] -= c * r1[k];
+        }
+        double alpha = dot(dctx, v, y);
+        double c2 = alpha / beta;
+        #pragma omp parallel for schedule(static)
+        for (long k = 0; k < n; ++k) y[k] -= c2 * r2[k];
+        double* t = r1; r1 = r2; r2 = t;                       /* r1 = move(r2) */
+        memcpy(r2, y, sizeof(double) * n);                     /* r2 = y; y = precond(r2) */
+        beta_old = beta;
+        beta = sqrt(dot(dctx, y, y));
+        tnorm += alpha * alpha + beta * beta + beta_old * beta_old;
+        eps_old = eps;
+        double delta = cs * dbar + sn * alpha;
+        double gbar = sn * dbar - cs * alpha;
+        eps = sn * beta;
+        dbar = -cs * beta;
+        double gamma = sqrt(gbar * gbar + beta * beta);
+        if (gamma < machine_epsilon) gamma = machine_epsilon;
+        cs = gbar / gamma;
+        sn = beta / gamma;
+        double phi = cs * phibar;
+        phibar *= sn;
+        t = w1; w1 = w2; w2 = w; w = t;                        /* w1 = w2; w2 = w */
+        double g = 1.0 / gamma;
+        #pragma omp parallel for schedule(static)
+        for (long k = 0; k < n; ++k) {
+            w[k] = g * ((v[k] - eps_old * w1[k]) - delta * w2[k]);
+            x[k] += phi * w[k];
+        }
+        if (phibar < tol * b_norm + tol) {
+            success = 1;
+            break;
+        }
+    }
+    free(r1); free(r2); free(y); free(v); free(w); free(w1); free(w2);
+    or_results res = {success, i, phibar};
+    return res;
+}
+
+/* include/pcg.hpp:59-97 with the identity-preconditioner conj_grad overloads (:20-25, :41-50) */
+or_results or_pcg(double* x, or_linop A, void* actx, const double* b, or_dotfn dot, void* dctx,
+                  long n, int max_iter, double tol)
+{
+    double* r = vnew(n);
+    double* p = vnew(n);
+    double* Ap = vnew(n);
+    A(actx, x, Ap);
+    #pragma omp parallel for schedule(static)
+    for (long k = 0; k < n; ++k) r[k] = b[k] - Ap[k];
+    double bnorm = sqrt(dot(dctx, b, b));
+    int success = 0;
+    double rho_prev = 0, rho = 0;
+    int i;
+    for (i = 0; i < max_iter; ++i) {
+        if (i == 0) {
+            memcpy(p, r, sizeof(double) * n);
+            rho = dot(dctx, r, r);
+        } else {
+            rho = dot(dctx, r, r);
+            double beta = rho / rho_prev;
+            #pragma omp parallel for schedule(static)
+            for (long k = 0; k < n; ++k) p[k] = r[k] + beta * p[k];
+        }
+        A(actx, p, Ap);
+        double alpha = rho / dot(dctx, p, Ap);
+        #pragma omp parallel for schedule(static)
+        for (long k = 0; k < n; ++k) {
+            x[k] += alpha * p[k];
+            r[k] -= alpha * Ap[k];
+        }
+        rho_prev = rho;
+        if (sqrt(rho) < tol * bnorm) {
+            success = 1;
+            break;
+        }
+    }
+    free(r); free(p); free(Ap);
+    or_results res = {success, i, sqrt(rho)};
+    return res;
+}
+
+/* ------------------------------------------------------------------ a15 */
+
+static void op_laplace(void* ctx, const double* in, double* out) { or_apply_laplace((const or_mesh*)ctx, in, out); }
+static double dot1(void* ctx, const double* a, const double* b) { return or_dot((const or_mesh*)ctx, a, b); }
+
+/* include/openmp_impl/poisson.hpp:17-59 */
+or_results or_poisson(const or_mesh* m, double* u, const double* f, int max_iter, double tol)
+{
+    size_t n = (size_t)m->n_el * m->N * m->N;
+    double* b = vnew((long)n);
+    or_gproj(m, f, b);
+    or_results r = or_pcg(u, op_laplace, (void*)m, b, dot1, (void*)m, (long)n, max_iter, tol);
+    free(b);
+    return r;
+}
+
+typedef struct { const or_mesh* m; const double* c; } helm_ctx;
+static void op_helm(void* ctx, const double* in, double* out)
+{
+    helm_ctx* h = (helm_ctx*)ctx;
+    or_apply_helmholtz(h->m, h->c, in, out);
+}
+
+/* include/openmp_impl/helmholtz.hpp:18-64 */
+or_results or_helmholtz(const or_mesh* m, double* u, const double* c, const double* f, int max_iter, double tol)
+{
+    size_t n = (size_t)m->n_el * m->N * m->N;
+    double* b = vnew((long)n);
+    or_gproj(m, f, b);
+    helm_ctx h = {m, c};
+    or_results r = or_minres(u, op_helm, &h, b, dot1, (void*)m, (long)n, max_iter, tol);
+    free(b);
+    return r;
+}
+
+/* two-plane (real, imaginary) vectors for the Schroedinger drivers */
+typedef struct { const or_mesh* m; const double* V; double alpha; size_t n; } schro_ctx;
+
+static void op_res(void* ctx, const double* in, double* out)
+{
+    schro_ctx* s = (schro_ctx*)ctx;
+    or_schro_res(s->m, s->V, s->alpha, in, in + s->n, out, out + s->n);
+}
+
+static double dot2(void* ctx, const double* a, const double* b)
+{
+    schro_ctx* s = (schro_ctx*)ctx;
+    return or_dot(s->m, a, b) + or_dot(s->m, a + s->n, b + s->n);
+}
+
+/* dt * f(q) */
+static void rhs_f(schro_ctx* s, double dt, const double* q, double* out)
+{
+    or_schro_f(s->m, s->V, q, q + s->n, out, out + s->n);
+    size_t n2 = 2 * s->n;
+    #pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n2; ++k) out[k] = dt * out[k];
+}
+
+/* include/openmp_impl/schrodinger.hpp:22-128 */
+int or_schrodinger_bdf2(const or_mesh* m, double* psi_re, double* psi_im, const double* V,
+                        double T, const or_solver_opts* opts, or_callback cb, void* user)
+{
+    size_t n = (size_t)m->n_el * m->N * m->N, n2 = 2 * n;
+    schro_ctx s = {m, V, opts->dt, n};
+    double* p = vnew((long)n2);
+    memcpy(p, psi_re, sizeof(double) * n);
+    memcpy(p + n, psi_im, sizeof(double) * n);
+    double* ps[2] = {vnew((long)n2), vnew((long)n2)};
+    double* b = vnew((long)n2);
+    int nps = 0;
+    int success = 1;
+    double t = 0;
+    int step = 0;
+    while (t < T) {
+        if (nps == 2) { double* q = ps[0]; ps[0] = ps[1]; ps[1] = q; nps = 1; } /* pop_front */
+        double* dst = ps[nps];
+        or_gproj(m, p, dst);                           /* proj(p), :69-78 */
+        or_gproj(m, p + n, dst + n);
+        for (size_t k = 0; k < n; ++k) dst[n + k] = -1.0 * dst[n + k];
+        ++nps;
+        or_results r;
+        if (nps == 1) {
+            r = or_minres(p, op_res, &s, ps[0], dot2, &s, (long)n2, opts->max_iter, opts->tol);
+            s.alpha = (2.0 / 3.0) * opts->dt;
+        } else {
+            const double c0 = -1.0 / 3.0, c1 = 4.0 / 3.0;
+            for (size_t k = 0; k < n2; ++k) b[k] = c0 * ps[0][k] + c1 * ps[1][k];
+            r = or_minres(p, op_res, &s, b, dot2, &s, (long)n2, opts->max_iter, opts->tol);
+        }
+        or_unmask(m, p);
+        or_unmask(m, p + n);
+        t += opts->dt;
+        success = r.success;
+        if (!success) break;
+        ++step;
+        if (cb) {
+            int it = r.n_iter;
+            if (cb(user, step, p, p + n, &it, 1)) break;
+        }
+    }
+    memcpy(psi_re, p, sizeof(double) * n);
+    memcpy(psi_im, p + n, sizeof(double) * n);
+    free(p); free(ps[0]); free(ps[1]); free(b);
+    return success;
+}
+
+/* v = p + sum_k c[k] * z[k], evaluated left to right like the reference's
+ * expression templates */
+static void combo(size_t n2, double* out, const double* p, int nz, const double* const* z, const double* c)
+{
+    #pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n2; ++k) {
+        double v = p[k];
+        for (int q = 0; q < nz; ++q) v = v + c[q] * z[q][k];
+        out[k] = v;
+    }
+}
+
+/* p += (c0 z0 + c1 z1 + ...) */
+static void accum(size_t n2, double* p, int nz, const double* const* z, const double* c)
+{
+    #pragma omp parallel for schedule(static)
+    for (size_t k = 0; k < n2; ++k) {
+        double v = c[0] * z[0][k];
+        for (int q = 1; q < nz; ++q) v = v + c[q] * z[q][k];
+        p[k] += v;
+    }
+}
+
+/* include/openmp_impl/schrodinger.hpp:138-285 */
+int or_schrodinger_dirk4s5(const or_mesh* m, double* psi_re, double* psi_im, const double* V,
+                           double T, const or_solver_opts* opts, or_callback cb, void* user)
+{
+    size_t n = (size_t)m->n_el * m->N * m->N, n2 = 2 * n;
+    schro_ctx s = {m, V, 0.25 * opts->dt, n};
+    double* p = vnew((long)n2);
+    memcpy(p, psi_re, sizeof(double) * n);
+    memcpy(p + n, psi_im, sizeof(double) * n);
+    double* v = vnew((long)n2);
+    double* rhs = vnew((long)n2);
+    double* z[5];
+    for (int k = 0; k < 5; ++k) z[k] = vnew((long)n2);
+    double pnorm = sqrt(dot2(&s, p, p));
+    (void)pnorm;
+    static const double a2[] = {0.5};
+    static const double a3[] = {17.0 / 50.0, -1.0 / 25.0};
+    static const double a4[] = {371.0 / 1360.0, -137.0 / 2720.0, 15.0 / 544.0};
+    static const double a5[] = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0};
+    static const double bb[] = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0, 0.25};
+    const double* arows[5] = {NULL, a2, a3, a4, a5};
+    double t = 0;
+    int success = 1;
+    int step = 0;
+    while (t < T) {
+        int iters[5] = {0, 0, 0, 0, 0};
+        for (int st = 0; st < 5; ++st) {
+            if (st == 0) rhs_f(&s, opts->dt, p, rhs);
+            else {
+                combo(n2, v, p, st, (const double* const*)z, arows[st]);
+                rhs_f(&s, opts->dt, v, rhs);
+            }
+            memset(z[st], 0, sizeof(double) * n2); /* zi = zeros */
+            or_results r = or_minres(z[st], op_res, &s, rhs, dot2, &s, (long)n2, opts->max_iter, opts->tol);
+            iters[st] = r.n_iter;
+            success = r.success;
+            if (!success) goto done;
+        }
+        accum(n2, p, 5, (const double* const*)z, bb);
+        or_unmask(m, p);
+        or_unmask(m, p + n);
+        t += opts->dt;
+        ++step;
+        if (cb && cb(user, step, p, p + n, iters, 5)) break;
+    }
+done:
+    memcpy(psi_re, p, sizeof(double) * n);
+    memcpy(psi_im, p + n, sizeof(double) * n);
+    free(p); free(v); free(rhs);
+    for (int k = 0; k < 5; ++k) free(z[k]);
+    return success;
+}
+
+/* include/openmp_impl/schrodinger.hpp:294-423 */
+int or_schrodinger_dirk4s3(const or_mesh* m, double* psi_re, double* psi_im, const double* V,
+                           double T, const or_solver_opts* opts, or_callback cb, void* user)
+{
+    const double gamma = cos(M_PI / 18.0) / sqrt(3.0) + 0.5;
+    const double delta = 1.0 / 6.0 / pow(2 * gamma - 1, 2);
+    size_t n = (size_t)m->n_el * m->N * m->N, n2 = 2 * n;
+    schro_ctx s = {m, V, gamma * opts->dt, n};
+    double* p = vnew((long)n2);
+    memcpy(p, psi_re, sizeof(double) * n);
+    memcpy(p + n, psi_im, sizeof(double) * n);
+    double* v = vnew((long)n2);
+    double* rhs = vnew((long)n2);
+    double* z[3];
+    for (int k = 0; k < 3; ++k) z[k] = vnew((long)n2);
+    const double a2[] = {0.5 - gamma};
+    const double a3[] = {2 * gamma, 1 - 4 * gamma};
+    const double bb[] = {delta, 1 - 2 * delta, delta};
+    const double* arows[3] = {NULL, a2, a3};
+    double t = 0;
+    int success = 1;
+    int step = 0;
+    while (t < T) {
+        int iters[3] = {0, 0, 0};
+        for (int st = 0; st < 3; ++st) {
+            if (st == 0) rhs_f(&s, opts->dt, p, rhs);
+            else {
+                combo(n2, v, p, st, (const double* const*)z, arows[st]);
+                rhs_f(&s, opts->dt, v, rhs);
+            }
+            memset(z[st], 0, sizeof(double) * n2);
+            or_results r = or_minres(z[st], op_res, &s, rhs, dot2, &s, (long)n2, opts->max_iter, opts->tol);
+            iters[st] = r.n_iter;
+            success = r.success;
+            if (!success) goto done;
+        }
+        accum(n2, p, 3, (const double* const*)z, bb);
+        or_unmask(m, p);
+        or_unmask(m, p + n);
+        t += opts->dt;
+        ++step;
+        if (cb && cb(user, step, p, p + n, iters, 3)) break;
+    }
+done:
+    memcpy(psi_re, p, sizeof(double) * n);
+    memcpy(psi_im, p + n, sizeof(double) * n);
+    free(p); free(v); free(rhs);
+    for (int k = 0; k < 3; ++k) free(z[k]);
+    return success;
+}

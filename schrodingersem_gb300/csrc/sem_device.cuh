@@ -1,0 +1,343 @@
+// Device-side building blocks for the sm_103a spectral-element kernels.
+//
+// Data layout: a field is E element blocks of N*N values, column-major
+// inside the block: node (i,j) of element e at flat index e*N*N + j*N + i
+// (the reference's std::vector<arma::Mat> laid end to end).
+#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include "sem_internal.h"
+
+namespace semgb {
+
+// ---------------------------------------------------------------- geometry
+// Elements per block-chunk (K) and threads per block (TPB) for each N: one
+// thread per element-local node, K elements side by side, TPB a multiple of
+// 32 chosen to waste as few lanes as possible.
+__host__ __device__ constexpr int geo_k(int N)
+{
+    return N <= 9 ? 256 / (N * N) : N == 10 ? 5 : N == 11 ? 4 : N <= 13 ? 3 : N <= 16 ? 2 : 1;
+}
+__host__ __device__ constexpr int geo_tpb(int N)
+{
+    return ((geo_k(N) * N * N + 31) / 32) * 32;
+}
+
+template <int OP>
+__host__ __device__ constexpr int op_nc()
+{
+    return (OP == OP_RES || OP == OP_F) ? 2 : 1;
+}
+
+template <typename T>
+struct Fac {
+    const T *g11, *g12, *g22, *mass;
+};
+
+template <typename T>
+__host__ __device__ inline Fac<T> fac_of(const DevMesh& m);
+template <>
+__host__ __device__ inline Fac<double> fac_of<double>(const DevMesh& m)
+{
+    return Fac<double>{m.g11, m.g12, m.g22, m.mass};
+}
+template <>
+__host__ __device__ inline Fac<float> fac_of<float>(const DevMesh& m)
+{
+    return Fac<float>{m.g11f, m.g12f, m.g22f, m.massf};
+}
+template <typename T>
+__device__ inline const T* dmat_of(const DevMesh& m);
+template <>
+__device__ inline const double* dmat_of<double>(const DevMesh& m) { return m.D64; }
+template <>
+__device__ inline const float* dmat_of<float>(const DevMesh& m) { return m.D32; }
+
+// ------------------------------------------------------- node classification
+// kind 0: element interior; 1: side sc, position k; 2: corner sc.
+struct NodeInfo {
+    int kind, sc, k, flags;
+};
+
+template <int N>
+__device__ __forceinline__ NodeInfo node_info(const DevMesh& m, int e, int i, int j)
+{
+    NodeInfo r;
+    const bool ib = (i == 0) | (i == N - 1);
+    const bool jb = (j == 0) | (j == N - 1);
+    r.k = 0;
+    if (ib && jb) {
+        r.kind = 2;
+        r.sc = (j == 0) ? (i == 0 ? 0 : 1) : (i == 0 ? 3 : 2);
+    } else if (jb) {
+        r.kind = 1;
+        r.sc = (j == 0) ? 0 : 2;
+        r.k = i;
+    } else if (ib) {
+        r.kind = 1;
+        r.sc = (i == N - 1) ? 1 : 3;
+        r.k = j;
+    } else {
+        r.kind = 0;
+        r.sc = 0;
+    }
+    r.flags = (r.kind == 0) ? 0 : __ldg(m.flags + e);
+    return r;
+}
+
+// is this copy the one the reference's dot() counts (dot.hpp:11-61)?
+__device__ __forceinline__ bool ni_owner(const NodeInfo& ni)
+{
+    if (ni.kind == 0) return true;
+    if (ni.kind == 1) return (ni.flags >> ni.sc) & 1;
+    return (ni.flags >> (8 + ni.sc)) & 1;
+}
+
+__device__ __forceinline__ bool ni_boundary(const NodeInfo& ni)
+{
+    if (ni.kind == 0) return false;
+    if (ni.kind == 1) return (ni.flags >> (4 + ni.sc)) & 1;
+    return (ni.flags >> (12 + ni.sc)) & 1;
+}
+
+// flat index whose value unmask() copies into this node: the owner copy for
+// non-owner copies of interior sides/corners (unmask.hpp:12-36), else itself.
+__device__ __forceinline__ long long ni_gather_src(const DevMesh& m, const NodeInfo& ni, int e,
+                                                   long long flat)
+{
+    if (ni.kind == 0 || ni_owner(ni) || ni_boundary(ni)) return flat;
+    if (ni.kind == 1)
+        return (long long)__ldg(m.side_base + 4 * e + ni.sc) +
+               (long long)ni.k * __ldg(m.side_step + 4 * e + ni.sc);
+    return __ldg(m.corner_src + 4 * e + ni.sc);
+}
+
+template <typename T>
+__device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
+
+// assembled value at a node (global_sum.hpp:13-63 + mask.hpp:16-28 by mode).
+// Values of other elements are read with ld.cg: inside the persistent
+// kernels they were written by other blocks in the previous phase.
+template <int N, typename T, int MODE>
+__device__ __forceinline__ T dss_value(const DevMesh& m, const T* Y, const NodeInfo& ni, int e,
+                                       long long flat)
+{
+    const T own = ldcg(Y + flat);
+    if (ni.kind == 0) return own;
+    if (ni_boundary(ni)) return MODE == DSS_SUM ? own : T(0);
+    if (MODE == DSS_MASK && !ni_owner(ni)) return T(0);
+    if (ni.kind == 1) {
+        const long long nf = (long long)__ldg(m.side_base + 4 * e + ni.sc) +
+                             (long long)ni.k * __ldg(m.side_step + 4 * e + ni.sc);
+        return own + ldcg(Y + nf);  // owner + other in either copy: commutative, same bits
+    }
+    const int node = __ldg(m.corner_node + 4 * e + ni.sc);
+    const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
+    T s = T(0);  // csum = 0, then += in connected_elements order (global_sum.hpp:56-59)
+    for (int q = q0; q < q1; ++q) s += ldcg(Y + __ldg(m.node_flat + q));
+    return s;
+}
+
+// ------------------------------------------------------------ element apply
+template <int N, typename T, int OP>
+struct ApplySmem {
+    static constexpr int NN = N * N;
+    static constexpr int K = geo_k(N);
+    static constexpr int NC = op_nc<OP>();
+    T D[NN];
+    T u[NC][K * NN];
+    T f1[NC][K * NN];
+    T f2[NC][K * NN];
+};
+
+template <int N, typename T, int OP>
+__device__ __forceinline__ void load_dmat(ApplySmem<N, T, OP>& s, const DevMesh& m)
+{
+    const T* D = dmat_of<T>(m);
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) s.D[t] = D[t];
+}
+
+// One block-wide pass of the fused element operator over elements
+// [e0, min(e0+K, e_end)).  Every thread of the block must call it (it holds
+// __syncthreads).  load(e,i,j,flat,u[NC]) supplies the node's input values;
+// store(e,i,j,flat,out[NC]) receives the element-local result.
+//
+// Weak Laplacian with premultiplied factors (glaplace.hpp:16-28 rewritten
+// with g11 = w_i w_j A, g12 = w_i w_j B, g22 = w_i w_j C):
+//   f1 = g11 u_xi - g12 u_eta,   f2 = g22 u_eta - g12 u_xi
+//   lap(i,j) = sum_k D(k,i) f1(k,j) + sum_k D(k,j) f2(i,k)
+// Mass term (W (u%V) W) % J = (w_i w_j J) V u.
+template <int N, typename T, int OP, class Load, class Store>
+__device__ __forceinline__ void apply_chunk(ApplySmem<N, T, OP>& s, const Fac<T>& fac,
+                                            const T* __restrict__ pot, T alpha, int e0, int e_end,
+                                            Load&& load, Store&& store)
+{
+    constexpr int NN = N * N;
+    constexpr int K = geo_k(N);
+    constexpr int NC = op_nc<OP>();
+    const int t = threadIdx.x;
+    const int le = t / NN;
+    const int node = t - le * NN;
+    const int i = node % N, j = node / N;
+    const int e = e0 + le;
+    const bool active = (le < K) && (e < e_end);
+    const long long flat = (long long)e * NN + node;
+    T u[NC];
+    T g11 = T(0), g12 = T(0), g22 = T(0), ms = T(0), pv = T(0);
+    if (active) {
+        if (OP != OP_MASS) {
+            g11 = __ldg(fac.g11 + flat);
+            g12 = __ldg(fac.g12 + flat);
+            g22 = __ldg(fac.g22 + flat);
+        }
+        if (OP != OP_LAPLACE) ms = __ldg(fac.mass + flat);
+        if (OP == OP_HELM || OP == OP_RES || OP == OP_F) pv = __ldg(pot + flat);
+        load(e, i, j, flat, u);
+    }
+    if (OP == OP_MASS) {
+        if (active) {
+            T o[NC];
+            o[0] = ms * u[0];
+            store(e, i, j, flat, o);
+        }
+        return;
+    }
+    if (active) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) s.u[c][le * NN + node] = u[c];
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* uc = &s.u[c][le * NN];
+            T ur = T(0), us = T(0);
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                ur = fma(s.D[i * N + k], uc[k + j * N], ur);  // (D u)(i,j)
+                us = fma(s.D[j * N + k], uc[i + k * N], us);  // (u D^T)(i,j)
+            }
+            s.f1[c][le * NN + node] = g11 * ur - g12 * us;
+            s.f2[c][le * NN + node] = g22 * us - g12 * ur;
+        }
+    }
+    __syncthreads();
+    if (active) {
+        T lap[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* f1 = &s.f1[c][le * NN];
+            const T* f2 = &s.f2[c][le * NN];
+            T a = T(0);
+#pragma unroll
+            for (int k = 0; k < N; ++k) a = fma(s.D[k * N + i], f1[k + j * N], a);
+#pragma unroll
+            for (int k = 0; k < N; ++k) a = fma(s.D[k * N + j], f2[i + k * N], a);
+            lap[c] = a;
+        }
+        T o[NC];
+        if (OP == OP_LAPLACE) {
+            o[0] = lap[0];
+        } else if (OP == OP_HELM) {
+            o[0] = lap[0] + (ms * pv) * u[0];
+        } else if (OP == OP_RES) {
+            const T mv = ms * pv;
+            const T Lv = lap[NC - 1] + mv * u[NC - 1];
+            const T Lu = lap[0] + mv * u[0];
+            o[0] = ms * u[0] + alpha * Lv;
+            o[NC - 1] = alpha * Lu - ms * u[NC - 1];
+        } else {  // OP_F
+            const T mv = ms * pv;
+            o[0] = -(lap[NC - 1] + mv * u[NC - 1]);
+            o[NC - 1] = -(lap[0] + mv * u[0]);
+        }
+        store(e, i, j, flat, o);
+    }
+    __syncthreads();
+}
+
+// --------------------------------------------------------------- reductions
+// block sum of a double, result returned to every thread (fixed order)
+__device__ __forceinline__ double block_sum(double v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        double s = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier for cooperatively launched kernels.  Every wait is
+// bounded: after timeout_ns the block records gs->err and returns false, so
+// no block can spin forever.  Returns true when all blocks arrived.
+__device__ __forceinline__ bool grid_barrier(GridSync* gs, long long timeout_ns)
+{
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned int* vgen = &gs->gen;
+        volatile int* verr = &gs->err;
+        const unsigned int g = *vgen;
+        __threadfence();
+        const unsigned int arrived = atomicAdd(&gs->count, 1u);
+        if (arrived == gridDim.x - 1) {
+            atomicExch(&gs->count, 0u);
+            __threadfence();
+            atomicAdd(&gs->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (*vgen == g) {
+                if (*verr) break;
+                if ((long long)(global_ns() - t0) > timeout_ns) {
+                    atomicExch(&gs->err, 1);
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *((volatile int*)&gs->err) == 0;
+}
+
+// all-reduce of one double across the grid: block sums to partials[slot][blk],
+// barrier, then every block sums the partials in the same fixed order.
+__device__ __forceinline__ double grid_sum(double v, double* partials, int slot, GridSync* gs,
+                                           long long timeout_ns, double* red, bool& ok)
+{
+    const double bs = block_sum(v, red);
+    const int G = gridDim.x;
+    if (threadIdx.x == 0) partials[(size_t)slot * G + blockIdx.x] = bs;
+    ok = grid_barrier(gs, timeout_ns);
+    if (threadIdx.x < 32) {
+        double s = 0.0;
+        for (int q = threadIdx.x; q < G; q += 32) s += __ldcg(partials + (size_t)slot * G + q);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (threadIdx.x == 0) red[33] = s;
+    }
+    __syncthreads();
+    const double r = red[33];
+    __syncthreads();
+    return r;
+}
+
+}  // namespace semgb

@@ -1,0 +1,1201 @@
+// Host side of the GB300 spectral-element library: mesh setup (topology,
+// LGL quadrature, metrics), device buffers, dispatch over the polynomial
+// degree, and every extern "C" entry point of include/sem_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <type_traits>
+#include <unordered_map>
+#include <vector>
+
+#include "sem_gb300.h"
+#include "sem_internal.h"
+
+using namespace semgb;
+
+// ------------------------------------------------------------------ errors
+static thread_local std::string g_last_error;
+
+static int fail(int code, const std::string& msg)
+{
+    g_last_error = msg;
+    return code;
+}
+
+#define SEM_CUDA(call)                                                                      \
+    do {                                                                                    \
+        cudaError_t e_ = (call);                                                            \
+        if (e_ != cudaSuccess)                                                              \
+            return fail(SEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class F>
+static cudaError_t dispatch_n(int N, F&& f)
+{
+    switch (N) {
+#define SEM_CASE(NV) \
+    case NV: return f(std::integral_constant<int, NV>{});
+        SEM_FOR_EACH_N(SEM_CASE)
+#undef SEM_CASE
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+// ------------------------------------------------------------ small kernels
+__global__ void k_axpby(long long n, double a, const double* __restrict__ x, double b,
+                        const double* __restrict__ y, double* __restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double v = a * x[i];
+        out[i] = y ? v + b * y[i] : v;
+    }
+}
+
+__global__ void k_lincomb(long long n, ZList zl, double* __restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double acc = zl.c[0] * zl.z[0][i];
+        for (int l = 1; l < zl.nz; ++l) acc = acc + zl.c[l] * zl.z[l][i];
+        out[i] = acc;
+    }
+}
+
+__global__ void k_to_f32(long long n, const double* __restrict__ a, float* __restrict__ b)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        b[i] = (float)a[i];
+}
+
+static int grid_1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 16); }
+
+// --------------------------------------------------------------- quadrature
+static double legendre(int n, double x)
+{
+    if (n == 0) return 1.0;
+    double p0 = 1.0, p1 = x;
+    for (int k = 1; k < n; ++k) {
+        const double p2 = ((2.0 * k + 1.0) * x * p1 - k * p0) / (k + 1.0);
+        p0 = p1;
+        p1 = p2;
+    }
+    return p1;
+}
+
+// LGL nodes and weights of degree p (N = p+1 values).  For p <= 8 the
+// reference's stated 15-digit nodes are used so the discretisation is the
+// reference's own (include/gauss_lobatto.hpp:49-58).  For p > 8 the interior
+// nodes, the roots of P_{p+1} - P_{p-1}, come from Newton's method started at
+// the Chebyshev-Gauss-Lobatto points.  Weights 2/(p(p+1) P_p(x)^2)
+// (include/gauss_lobatto.hpp:116-123).
+static void lgl(int p, std::vector<double>& x, std::vector<double>& w)
+{
+    static const std::vector<std::vector<double>> tab = {
+        {},
+        {-1, 1},
+        {-1, 0, 1},
+        {-1, -0.447213595499958, 0.447213595499958, 1},
+        {-1, -0.654653670707977, 0, 0.654653670707977, 1},
+        {-1, -0.765055323929465, -0.285231516480645, 0.285231516480645, 0.765055323929465, 1},
+        {-1, -0.830223896278567, -0.468848793470714, 0.0, 0.468848793470714, 0.830223896278567, 1},
+        {-1, -0.871740148509607, -0.591700181433142, -0.209299217902479, 0.2092992179024789,
+         0.591700181433142, 0.871740148509607, 1},
+        {-1, -0.899757995411460, -0.677186279510738, -0.363117463826178, 0, 0.363117463826178,
+         0.677186279510738, 0.899757995411460, 1}};
+    x.assign(p + 1, 0.0);
+    w.assign(p + 1, 0.0);
+    if (p <= 8) {
+        x = tab[p];
+    } else {
+        const int h = (p - 1) / 2;  // interior roots strictly below zero
+        std::vector<double> neg(h);
+        for (int k = 0; k < h; ++k) {
+            double z = -std::cos(M_PI * (k + 1) / p);
+            for (int it = 0; it < 100; ++it) {
+                const double q = legendre(p + 1, z) - legendre(p - 1, z);
+                const double dq = (2.0 * p + 1.0) * legendre(p, z);
+                const double dz = q / dq;
+                z -= dz;
+                if (std::fabs(dz) < 1e-17) break;
+            }
+            neg[k] = z;
+        }
+        int c = 0;
+        x[c++] = -1;
+        for (int k = 0; k < h; ++k) x[c++] = neg[k];
+        if (p % 2 == 0) x[c++] = 0;
+        for (int k = h - 1; k >= 0; --k) x[c++] = -neg[k];
+        x[c++] = 1;
+    }
+    w[0] = 2.0 / (p * (p + 1));
+    w[p] = w[0];
+    for (int i = 0; i < p / 2 + 1; ++i) {
+        const double pn = legendre(p, x[i]);
+        w[i] = 2.0 / (p * (p + 1) * (pn * pn));
+        w[p - i] = w[i];
+    }
+}
+
+// Barycentric differentiation matrix, column-major like arma
+// (include/derivative_matrix.hpp:12-38 -- the same formula, kept identical
+// because parity of every apply depends on it).
+static std::vector<double> dmatrix(const std::vector<double>& x)
+{
+    const int n = (int)x.size();
+    std::vector<double> bw(n, 1.0), D(n * n, 0.0);
+    for (int i = 0; i < n; ++i) {
+        for (int j = 0; j < n; ++j)
+            if (i != j) bw[i] *= x[i] - x[j];
+        bw[i] = 1 / bw[i];
+    }
+    for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j)
+            if (j != i) {
+                D[i + j * n] = (bw[j] / bw[i]) / (x[i] - x[j]);
+                D[i + i * n] -= D[i + j * n];
+            }
+    return D;
+}
+
+// ------------------------------------------------------------------ context
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+struct sem_ctx {
+    int p = 0, N = 0, E = 0, n_nodes = 0, n_edges = 0, n_int_edges = 0, n_bnd_edges = 0,
+        n_bnd_nodes = 0;
+    long long n = 0, dof = 0;
+    unsigned flags = 0;
+    std::vector<double> x, w, D;           // D column-major
+    std::vector<double> coords;            // [n_nodes][2]
+    std::vector<int> elements;             // [E][4]
+    std::vector<double> J, A, B, C;        // host metrics [E][N][N]
+    DevMesh dm;
+    std::vector<void*> owned;              // device allocations freed at destroy
+    cudaStream_t stream = nullptr;
+    int device = 0, sms = 0;
+    // options
+    int prec = SEM_PREC_FP64;
+    double inner_tol = 1e-4;
+    int guess = SEM_GUESS_ZERO;
+    double timeout_ms = 2000.0;
+    int max_refine = 50;
+    sem_stats stats{};
+    // workspace
+    std::unordered_map<std::string, DevBuf> ws;
+    SolveOut* h_out = nullptr;  // pinned
+    GridSync* h_sync = nullptr; // pinned
+    double* h_part = nullptr;   // pinned partials for dots
+};
+
+static int ctx_alloc(sem_ctx* c, void** p, size_t bytes)
+{
+    cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));
+    if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    c->owned.push_back(*p);
+    return SEM_OK;
+}
+
+template <class T>
+static int upload(sem_ctx* c, const std::vector<T>& v, const T** out)
+{
+    void* p = nullptr;
+    int s = ctx_alloc(c, &p, v.size() * sizeof(T));
+    if (s) return s;
+    if (!v.empty()) SEM_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    *out = (const T*)p;
+    return SEM_OK;
+}
+
+// named workspace buffer of at least `bytes`, allocated on first use
+static int wsbuf(sem_ctx* c, const char* name, size_t bytes, void** out)
+{
+    DevBuf& b = c->ws[name];
+    if (b.bytes < bytes) {
+        if (b.p) cudaFree(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+        cudaError_t e = cudaMalloc(&b.p, std::max<size_t>(bytes, 16));
+        if (e != cudaSuccess)
+            return fail(SEM_ERR_CUDA, std::string("cudaMalloc(workspace): ") + cudaGetErrorString(e));
+        b.bytes = bytes;
+    }
+    *out = b.p;
+    return SEM_OK;
+}
+
+template <class T>
+static int wsget(sem_ctx* c, const char* name, size_t count, T** out)
+{
+    void* p = nullptr;
+    int s = wsbuf(c, name, count * sizeof(T), &p);
+    *out = (T*)p;
+    return s;
+}
+
+static bool is_device_ptr(const void* p)
+{
+    if (!p) return false;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Build topology (include/load_mesh.hpp:146-206) and metrics
+// (include/Quad.hpp:27-55), upload everything.
+static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n_el,
+                     const int* elements, unsigned flags)
+{
+    if (p < 1 || p > MAX_N - 1) return fail(SEM_ERR_ARG, "polynomial degree must be 1..16");
+    if (n_nodes <= 0 || n_el <= 0 || !coords || !elements) return fail(SEM_ERR_ARG, "empty mesh");
+    const int N = p + 1, NN = N * N;
+    if ((long long)n_el * NN >= (1LL << 31)) return fail(SEM_ERR_UNSUPPORTED, "mesh too large for 32-bit node indices");
+    c->p = p;
+    c->N = N;
+    c->E = n_el;
+    c->n_nodes = n_nodes;
+    c->n = (long long)n_el * NN;
+    c->flags = flags;
+    c->coords.assign(coords, coords + 2 * (size_t)n_nodes);
+    c->elements.assign(elements, elements + 4 * (size_t)n_el);
+    for (int k = 0; k < 4 * n_el; ++k)
+        if (elements[k] < 0 || elements[k] >= n_nodes) return fail(SEM_ERR_MESH, "corner id out of range");
+    for (int e = 0; e < n_el; ++e)
+        for (int a = 0; a < 4; ++a)
+            for (int b = a + 1; b < 4; ++b)
+                if (elements[4 * e + a] == elements[4 * e + b])
+                    return fail(SEM_ERR_MESH, "element " + std::to_string(e) + " repeats a corner");
+    lgl(p, c->x, c->w);
+    c->D = dmatrix(c->x);
+
+    // unique edges keyed by the sorted corner pair; first element seen owns it
+    static const int emap1[] = {0, 1, 3, 0}, emap2[] = {1, 2, 2, 3};
+    struct Ed { int el[2]; int side[2]; };  // side: 0..3, el[1] = -1 on the boundary; rev flag below
+    std::vector<Ed> edges;
+    std::vector<char> rev;
+    edges.reserve(2 * (size_t)n_el + 4);
+    std::unordered_map<long long, int> key2e;
+    key2e.reserve(4 * (size_t)n_el);
+    for (int e = 0; e < n_el; ++e)
+        for (int s = 0; s < 4; ++s) {
+            const int a = elements[4 * e + emap1[s]], b = elements[4 * e + emap2[s]];
+            const long long key = (long long)std::min(a, b) * n_nodes + std::max(a, b);
+            auto it = key2e.find(key);
+            if (it == key2e.end()) {
+                key2e.emplace(key, (int)edges.size());
+                edges.push_back(Ed{{e, -1}, {s, -1}});
+                rev.push_back(0);
+            } else {
+                Ed& ed = edges[it->second];
+                if (ed.el[1] != -1) return fail(SEM_ERR_MESH, "an edge is shared by more than two elements");
+                const int n1 = elements[4 * ed.el[0] + emap1[ed.side[0]]];
+                ed.el[1] = e;
+                ed.side[1] = s;
+                rev[it->second] = (a == n1) ? 0 : 1;  // load_mesh.hpp:164-171
+            }
+        }
+    c->n_edges = (int)edges.size();
+    std::vector<int> fl(n_el, 0), sbase(4 * (size_t)n_el, -1), sstep(4 * (size_t)n_el, 0);
+    std::vector<char> node_bnd(n_nodes, 0);
+    auto side_pos = [&](int e, int s, int k) -> long long {  // flat index of node k on side s
+        const long long b = (long long)e * NN;
+        switch (s) {
+            case 0: return b + k;
+            case 1: return b + (N - 1) + (long long)k * N;
+            case 2: return b + k + (long long)(N - 1) * N;
+            default: return b + (long long)k * N;
+        }
+    };
+    for (size_t q = 0; q < edges.size(); ++q) {
+        const Ed& ed = edges[q];
+        if (ed.el[1] < 0) {
+            ++c->n_bnd_edges;
+            fl[ed.el[0]] |= (1 << ed.side[0]) | (16 << ed.side[0]);
+            node_bnd[elements[4 * ed.el[0] + emap1[ed.side[0]]]] = 1;
+            node_bnd[elements[4 * ed.el[0] + emap2[ed.side[0]]]] = 1;
+            continue;
+        }
+        ++c->n_int_edges;
+        fl[ed.el[0]] |= (1 << ed.side[0]);
+        for (int h = 0; h < 2; ++h) {
+            const int e = ed.el[h], s = ed.side[h];
+            const int eo = ed.el[1 - h], so = ed.side[1 - h];
+            // node k of (e,s) pairs with node k (same orientation) or N-1-k of (eo,so)
+            if (!rev[q]) {
+                sbase[4 * e + s] = (int)side_pos(eo, so, 0);
+                sstep[4 * e + s] = (int)(side_pos(eo, so, 1) - side_pos(eo, so, 0));
+            } else {
+                sbase[4 * e + s] = (int)side_pos(eo, so, N - 1);
+                sstep[4 * e + s] = -(int)(side_pos(eo, so, 1) - side_pos(eo, so, 0));
+            }
+        }
+    }
+    // corner copies in element order (load_mesh.hpp:123-143)
+    static const int cmi[] = {0, 1, 1, 0}, cmj[] = {0, 0, 1, 1};
+    std::vector<int> nptr(n_nodes + 1, 0), nflat(4 * (size_t)n_el), cnode(4 * (size_t)n_el),
+        csrc(4 * (size_t)n_el);
+    for (int k = 0; k < 4 * n_el; ++k) nptr[elements[k] + 1]++;
+    for (int k = 0; k < n_nodes; ++k) nptr[k + 1] += nptr[k];
+    std::vector<int> fill(n_nodes, 0);
+    for (int e = 0; e < n_el; ++e)
+        for (int cc = 0; cc < 4; ++cc) {
+            const int node = elements[4 * e + cc];
+            const int flat = e * NN + cmi[cc] * (N - 1) + cmj[cc] * (N - 1) * N;
+            nflat[nptr[node] + fill[node]++] = flat;
+            cnode[4 * e + cc] = node;
+        }
+    for (int e = 0; e < n_el; ++e)
+        for (int cc = 0; cc < 4; ++cc) {
+            const int node = cnode[4 * e + cc];
+            const int flat = e * NN + cmi[cc] * (N - 1) + cmj[cc] * (N - 1) * N;
+            csrc[4 * e + cc] = nflat[nptr[node]];
+            if (nflat[nptr[node]] == flat) fl[e] |= (256 << cc);
+            if (node_bnd[node]) fl[e] |= (4096 << cc);
+        }
+    for (int k = 0; k < n_nodes; ++k) c->n_bnd_nodes += node_bnd[k];
+    c->dof = (long long)n_nodes + (long long)c->n_edges * (N - 2) + (long long)n_el * (N - 2) * (N - 2);
+
+    // metrics, include/Quad.hpp:39-54 (C as the reference writes it unless corrected)
+    const bool corrected = (flags & SEM_FLAG_METRIC_CORRECTED) != 0;
+    c->J.assign(c->n, 0.0);
+    c->A.assign(c->n, 0.0);
+    c->B.assign(c->n, 0.0);
+    c->C.assign(c->n, 0.0);
+    std::vector<double> g11(c->n), g12(c->n), g22(c->n), ms(c->n);
+    const std::vector<double>& z = c->x;
+    for (int e = 0; e < n_el; ++e) {
+        double xs[4], ys[4];
+        for (int k = 0; k < 4; ++k) {
+            xs[k] = coords[2 * elements[4 * e + k]];
+            ys[k] = coords[2 * elements[4 * e + k] + 1];
+        }
+        double Xxi[MAX_N], Yxi[MAX_N], Xeta[MAX_N], Yeta[MAX_N];
+        for (int i = 0; i < N; ++i) {
+            Xxi[i] = 0.25 * ((1 - z[i]) * (xs[1] - xs[0]) + (1 + z[i]) * (xs[2] - xs[3]));
+            Yxi[i] = 0.25 * ((1 - z[i]) * (ys[1] - ys[0]) + (1 + z[i]) * (ys[2] - ys[3]));
+            Xeta[i] = 0.25 * ((1 - z[i]) * (xs[3] - xs[0]) + (1 + z[i]) * (xs[2] - xs[1]));
+            Yeta[i] = 0.25 * ((1 - z[i]) * (ys[3] - ys[0]) + (1 + z[i]) * (ys[2] - ys[1]));
+        }
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                const size_t k = (size_t)e * NN + i + (size_t)j * N;
+                const double Jv = Xxi[j] * Yeta[i] - Xeta[i] * Yxi[j];
+                const double Av = (Yeta[i] * Yeta[i] + Xeta[i] * Xeta[i]) / Jv;
+                const double Bv = (Yeta[i] * Yxi[j] + Xeta[i] * Xxi[j]) / Jv;
+                const double yx = corrected ? Yxi[j] : Yxi[i];
+                const double Cv = (yx * yx + Xxi[j] * Xxi[j]) / Jv;
+                c->J[k] = Jv;
+                c->A[k] = Av;
+                c->B[k] = Bv;
+                c->C[k] = Cv;
+                const double ww = c->w[i] * c->w[j];
+                g11[k] = ww * Av;
+                g12[k] = ww * Bv;
+                g22[k] = ww * Cv;
+                ms[k] = ww * Jv;
+            }
+    }
+    // device copies
+    DevMesh& d = c->dm;
+    d.N = N;
+    d.E = n_el;
+    d.n_nodes = n_nodes;
+    d.n = c->n;
+    std::vector<double> Drow(NN);
+    std::vector<float> Drowf(NN);
+    for (int i = 0; i < N; ++i)
+        for (int k = 0; k < N; ++k) {
+            Drow[i * N + k] = c->D[i + k * N];
+            Drowf[i * N + k] = (float)c->D[i + k * N];
+        }
+    auto tof = [](const std::vector<double>& v) {
+        std::vector<float> f(v.size());
+        for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
+        return f;
+    };
+    int s = 0;
+    if ((s = upload(c, fl, &d.flags)) || (s = upload(c, sbase, &d.side_base)) ||
+        (s = upload(c, sstep, &d.side_step)) || (s = upload(c, csrc, &d.corner_src)) ||
+        (s = upload(c, cnode, &d.corner_node)) || (s = upload(c, nptr, &d.node_ptr)) ||
+        (s = upload(c, nflat, &d.node_flat)) || (s = upload(c, Drow, &d.D64)) ||
+        (s = upload(c, Drowf, &d.D32)) || (s = upload(c, g11, &d.g11)) || (s = upload(c, g12, &d.g12)) ||
+        (s = upload(c, g22, &d.g22)) || (s = upload(c, ms, &d.mass)) ||
+        (s = upload(c, tof(g11), &d.g11f)) || (s = upload(c, tof(g12), &d.g12f)) ||
+        (s = upload(c, tof(g22), &d.g22f)) || (s = upload(c, tof(ms), &d.massf)))
+        return s;
+    SEM_CUDA(cudaMallocHost((void**)&c->h_out, sizeof(SolveOut)));
+    SEM_CUDA(cudaMallocHost((void**)&c->h_sync, sizeof(GridSync)));
+    SEM_CUDA(cudaMallocHost((void**)&c->h_part, sizeof(double) * 152 * 64));
+    return SEM_OK;
+}
+
+// ------------------------------------------------------------ C ABI: misc
+extern "C" int sem_version(void) { return SEM_GB300_VERSION; }
+
+extern "C" const char* sem_status_string(int s)
+{
+    switch (s) {
+        case SEM_OK: return "ok";
+        case SEM_ERR_ARG: return "invalid argument";
+        case SEM_ERR_CUDA: return "CUDA error";
+        case SEM_ERR_MESH: return "invalid mesh";
+        case SEM_ERR_IO: return "mesh folder unreadable";
+        case SEM_ERR_DEVICE_WAIT: return "device-side wait timed out";
+        case SEM_ERR_UNSUPPORTED: return "unsupported";
+        case SEM_ERR_NO_DEVICE: return "no CUDA device";
+        default: return "unknown status";
+    }
+}
+
+extern "C" const char* sem_last_error(void) { return g_last_error.c_str(); }
+
+// ------------------------------------------------------------ C ABI: mesh
+extern "C" int sem_ctx_create(sem_ctx** out, int p, int n_nodes, const double* coords, int n_el,
+                              const int* elements, unsigned flags)
+{
+    if (!out) return fail(SEM_ERR_ARG, "ctx pointer is null");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SEM_ERR_NO_DEVICE, "no CUDA device visible");
+    }
+    sem_ctx* c = new sem_ctx();
+    cudaGetDevice(&c->device);
+    cudaDeviceGetAttribute(&c->sms, cudaDevAttrMultiProcessorCount, c->device);
+    int s = build_ctx(c, p, n_nodes, coords, n_el, elements, flags);
+    if (s) {
+        sem_ctx_destroy(c);
+        return s;
+    }
+    *out = c;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_load(sem_ctx** out, int p, const char* folder, unsigned flags)
+{
+    if (!folder) return fail(SEM_ERR_ARG, "folder is null");
+    std::string f(folder);
+    std::ifstream info(f + "/info.txt");
+    if (!info.is_open()) return fail(SEM_ERR_IO, "could not open info file.");  // load_mesh.hpp:92-93
+    int n_nodes = 0, n_el = 0;
+    info >> n_nodes >> n_el;
+    if (n_nodes <= 0 || n_el <= 0) return fail(SEM_ERR_IO, "bad info.txt");
+    std::ifstream co(f + "/coordinates.txt");
+    if (!co.is_open()) return fail(SEM_ERR_IO, "could not open coordinate file.");
+    std::vector<double> coords(2 * (size_t)n_nodes);
+    for (auto& v : coords)
+        if (!(co >> v)) return fail(SEM_ERR_IO, "coordinates.txt too short");
+    std::ifstream el(f + "/elements.txt");
+    if (!el.is_open()) return fail(SEM_ERR_IO, "could not open element file.");
+    std::vector<int> elements(4 * (size_t)n_el);
+    for (auto& v : elements)
+        if (!(el >> v)) return fail(SEM_ERR_IO, "elements.txt too short");
+    return sem_ctx_create(out, p, n_nodes, coords.data(), n_el, elements.data(), flags);
+}
+
+extern "C" int sem_ctx_destroy(sem_ctx* c)
+{
+    if (!c) return SEM_OK;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    else cudaDeviceSynchronize();
+    for (void* p : c->owned) cudaFree(p);
+    for (auto& kv : c->ws)
+        if (kv.second.p) cudaFree(kv.second.p);
+    if (c->h_out) cudaFreeHost(c->h_out);
+    if (c->h_sync) cudaFreeHost(c->h_sync);
+    if (c->h_part) cudaFreeHost(c->h_part);
+    delete c;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_get_info(const sem_ctx* c, sem_mesh_info* info)
+{
+    if (!c || !info) return fail(SEM_ERR_ARG, "null argument");
+    info->p = c->p;
+    info->N = c->N;
+    info->n_elements = c->E;
+    info->n_nodes = c->n_nodes;
+    info->n_edges = c->n_edges;
+    info->n_interior_edges = c->n_int_edges;
+    info->n_boundary_edges = c->n_bnd_edges;
+    info->n_boundary_nodes = c->n_bnd_nodes;
+    info->n_local = c->n;
+    info->dof = c->dof;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_set_stream(sem_ctx* c, void* st)
+{
+    if (!c) return fail(SEM_ERR_ARG, "null ctx");
+    c->stream = (cudaStream_t)st;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
+{
+    if (!c) return fail(SEM_ERR_ARG, "null ctx");
+    switch (opt) {
+        case SEM_OPT_SOLVE_PRECISION:
+            if (v != SEM_PREC_FP64 && v != SEM_PREC_MIXED) return fail(SEM_ERR_ARG, "bad precision");
+            c->prec = (int)v;
+            return SEM_OK;
+        case SEM_OPT_INNER_TOL:
+            if (!(v > 0 && v < 1)) return fail(SEM_ERR_ARG, "inner tolerance must be in (0,1)");
+            c->inner_tol = v;
+            return SEM_OK;
+        case SEM_OPT_STAGE_GUESS:
+            if (v != SEM_GUESS_ZERO && v != SEM_GUESS_EXTRAPOLATE && v != SEM_GUESS_LEARNED)
+                return fail(SEM_ERR_ARG, "bad guess mode");
+            c->guess = (int)v;
+            return SEM_OK;
+        case SEM_OPT_WAIT_TIMEOUT_MS:
+            if (!(v > 0)) return fail(SEM_ERR_ARG, "timeout must be positive");
+            c->timeout_ms = v;
+            return SEM_OK;
+        case SEM_OPT_MAX_REFINE:
+            if (!(v >= 1)) return fail(SEM_ERR_ARG, "max refine must be >= 1");
+            c->max_refine = (int)v;
+            return SEM_OK;
+        default: return fail(SEM_ERR_ARG, "unknown option");
+    }
+}
+
+extern "C" int sem_ctx_get_stats(const sem_ctx* c, sem_stats* s)
+{
+    if (!c || !s) return fail(SEM_ERR_ARG, "null argument");
+    *s = c->stats;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_get_quadrature(const sem_ctx* c, double* x, double* w, double* D)
+{
+    if (!c) return fail(SEM_ERR_ARG, "null ctx");
+    if (x) std::memcpy(x, c->x.data(), sizeof(double) * c->N);
+    if (w) std::memcpy(w, c->w.data(), sizeof(double) * c->N);
+    if (D) std::memcpy(D, c->D.data(), sizeof(double) * c->N * c->N);
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_get_metrics(const sem_ctx* c, double* J, double* A, double* B, double* C)
+{
+    if (!c) return fail(SEM_ERR_ARG, "null ctx");
+    const size_t b = sizeof(double) * c->n;
+    if (J) std::memcpy(J, c->J.data(), b);
+    if (A) std::memcpy(A, c->A.data(), b);
+    if (B) std::memcpy(B, c->B.data(), b);
+    if (C) std::memcpy(C, c->C.data(), b);
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_get_node_coords(const sem_ctx* c, double* X, double* Y)
+{
+    if (!c || !X || !Y) return fail(SEM_ERR_ARG, "null argument");
+    const int N = c->N;
+    for (int e = 0; e < c->E; ++e) {
+        double xs[4], ys[4];
+        for (int k = 0; k < 4; ++k) {
+            xs[k] = c->coords[2 * c->elements[4 * e + k]];
+            ys[k] = c->coords[2 * c->elements[4 * e + k] + 1];
+        }
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                const double xi = c->x[i], eta = c->x[j];
+                const size_t k = (size_t)e * N * N + i + (size_t)j * N;
+                X[k] = 0.25 * (xs[0] * (1 - xi) * (1 - eta) + xs[1] * (1 + xi) * (1 - eta) +
+                               xs[2] * (1 + xi) * (1 + eta) + xs[3] * (1 - xi) * (1 + eta));
+                Y[k] = 0.25 * (ys[0] * (1 - xi) * (1 - eta) + ys[1] * (1 + xi) * (1 - eta) +
+                               ys[2] * (1 + xi) * (1 + eta) + ys[3] * (1 - xi) * (1 + eta));
+            }
+    }
+    return SEM_OK;
+}
+
+// --------------------------------------------------- C ABI: gather-scatter
+#define SEM_CHECK_CTX(c) \
+    if (!(c)) return fail(SEM_ERR_ARG, "null ctx")
+#define SEM_LAUNCH(expr)                                                                       \
+    do {                                                                                       \
+        cudaError_t e_ = (expr);                                                               \
+        if (e_ != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+extern "C" int sem_unmask(sem_ctx* c, double* a)
+{
+    SEM_CHECK_CTX(c);
+    if (!a) return fail(SEM_ERR_ARG, "null field");
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) { return launch_unmask<decltype(nv)::value>(c->dm, false, a, c->stream); }));
+    return SEM_OK;
+}
+
+extern "C" int sem_mask(sem_ctx* c, double* a)
+{
+    SEM_CHECK_CTX(c);
+    if (!a) return fail(SEM_ERR_ARG, "null field");
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) { return launch_mask<decltype(nv)::value>(c->dm, false, a, c->stream); }));
+    return SEM_OK;
+}
+
+extern "C" int sem_global_sum(sem_ctx* c, double* a)
+{
+    SEM_CHECK_CTX(c);
+    if (!a) return fail(SEM_ERR_ARG, "null field");
+    double* tmp = nullptr;
+    int s = wsget(c, "gs_tmp", c->n, &tmp);
+    if (s) return s;
+    SEM_CUDA(cudaMemcpyAsync(tmp, a, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dss<decltype(nv)::value>(c->dm, false, DSS_SUM, 1.0, tmp, a, c->stream);
+    }));
+    return SEM_OK;
+}
+
+static int dot_dev(sem_ctx* c, const double* a, const double* b, double* result)
+{
+    double* part = nullptr;
+    int s = wsget(c, "dot_part", 152 * 64, &part);
+    if (s) return s;
+    int used = 0;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dot<decltype(nv)::value>(c->dm, a, b, part, 152 * 64, &used, c->stream);
+    }));
+    SEM_CUDA(cudaMemcpyAsync(c->h_part, part, sizeof(double) * used, cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    double acc = 0.0;
+    for (int i = 0; i < used; ++i) acc += c->h_part[i];
+    *result = acc;
+    return SEM_OK;
+}
+
+extern "C" int sem_dot(sem_ctx* c, const double* a, const double* b, double* result)
+{
+    SEM_CHECK_CTX(c);
+    if (!a || !b || !result) return fail(SEM_ERR_ARG, "null argument");
+    return dot_dev(c, a, b, result);
+}
+
+extern "C" int sem_vec_axpby(sem_ctx* c, long long n, double a, const double* x, double b,
+                             const double* y, double* out)
+{
+    SEM_CHECK_CTX(c);
+    if (n < 0 || (n > 0 && (!x || !out))) return fail(SEM_ERR_ARG, "bad vector arguments");
+    if (n == 0) return SEM_OK;
+    k_axpby<<<grid_1d(n), 256, 0, c->stream>>>(n, a, x, b, y, out);
+    SEM_CUDA(cudaGetLastError());
+    return SEM_OK;
+}
+
+// --------------------------------------------------------- C ABI: operators
+// element-local op (input gathered with unmask semantics), then DSS + mask
+static int apply_galerkin(sem_ctx* c, int op, const double* pot, double alpha, const double* in0,
+                          const double* in1, double* out0, double* out1, double scale = 1.0)
+{
+    const int nc = (op == OP_RES || op == OP_F) ? 2 : 1;
+    double* Y = nullptr;
+    int s = wsget(c, "apply_Y", 2 * c->n, &Y);
+    if (s) return s;
+    double* Y1 = Y + c->n;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_apply<decltype(nv)::value>(c->dm, op, false, pot, alpha, in0, in1, Y, Y1, true, c->stream);
+    }));
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dss<decltype(nv)::value>(c->dm, false, DSS_MASK, scale, Y, out0, c->stream);
+    }));
+    if (nc == 2)
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_dss<decltype(nv)::value>(c->dm, false, DSS_MASK, scale, Y1, out1, c->stream);
+        }));
+    c->stats.fp64_applies++;
+    return SEM_OK;
+}
+
+extern "C" int sem_gproj(sem_ctx* c, const double* u, double* out)
+{
+    SEM_CHECK_CTX(c);
+    if (!u || !out) return fail(SEM_ERR_ARG, "null field");
+    return apply_galerkin(c, OP_MASS, nullptr, 0.0, u, nullptr, out, nullptr);
+}
+
+extern "C" int sem_apply_laplace(sem_ctx* c, const double* u, double* out)
+{
+    SEM_CHECK_CTX(c);
+    if (!u || !out) return fail(SEM_ERR_ARG, "null field");
+    return apply_galerkin(c, OP_LAPLACE, nullptr, 0.0, u, nullptr, out, nullptr);
+}
+
+extern "C" int sem_apply_helmholtz(sem_ctx* c, const double* cf, const double* u, double* out)
+{
+    SEM_CHECK_CTX(c);
+    if (!cf || !u || !out) return fail(SEM_ERR_ARG, "null field");
+    return apply_galerkin(c, OP_HELM, cf, 0.0, u, nullptr, out, nullptr);
+}
+
+extern "C" int sem_apply_schro_res(sem_ctx* c, const double* V, double alpha, const double* qr,
+                                   const double* qi, double* yr, double* yi)
+{
+    SEM_CHECK_CTX(c);
+    if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
+    return apply_galerkin(c, OP_RES, V, alpha, qr, qi, yr, yi);
+}
+
+extern "C" int sem_apply_schro_f(sem_ctx* c, const double* V, const double* qr, const double* qi,
+                                 double* yr, double* yi)
+{
+    SEM_CHECK_CTX(c);
+    if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
+    return apply_galerkin(c, OP_F, V, 0.0, qr, qi, yr, yi);
+}
+
+extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, const float* qr,
+                                       const float* qi, float* yr, float* yi)
+{
+    SEM_CHECK_CTX(c);
+    if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
+    float* Y = nullptr;
+    int s = wsget(c, "apply_Yf", 2 * c->n, &Y);
+    if (s) return s;
+    float* Y1 = Y + c->n;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_apply<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, Y, Y1, true, c->stream);
+    }));
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dss<decltype(nv)::value>(c->dm, true, DSS_MASK, 1.0, Y, yr, c->stream);
+    }));
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dss<decltype(nv)::value>(c->dm, true, DSS_MASK, 1.0, Y1, yi, c->stream);
+    }));
+    c->stats.fp32_applies++;
+    return SEM_OK;
+}
+
+// ------------------------------------------------------ C ABI: Krylov solvers
+static int krylov_work(sem_ctx* c, int nc, KrylovWork<double>* w, GridSync** sync, SolveOut** out)
+{
+    const size_t v = (size_t)nc * c->n;
+    const char* ln[3] = {"kr_L0", "kr_L1", "kr_L2"};
+    const char* wn[3] = {"kr_W0", "kr_W1", "kr_W2"};
+    const char* yn[2] = {"kr_Y0", "kr_Y1"};
+    int s = 0;
+    for (int k = 0; k < 3; ++k) {
+        if ((s = wsget(c, ln[k], v, &w->L[k]))) return s;
+        if ((s = wsget(c, wn[k], v, &w->W[k]))) return s;
+    }
+    for (int k = 0; k < 2; ++k)
+        if ((s = wsget(c, yn[k], v, &w->Y[k]))) return s;
+    if ((s = wsget(c, "kr_part", 2 * 152 * 64, &w->partials))) return s;
+    if ((s = wsget(c, "kr_sync", 1, sync))) return s;
+    if ((s = wsget(c, "kr_out", 1, out))) return s;
+    return SEM_OK;
+}
+
+static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
+                      const double* const b[2], int maxit, double tol, int x_is_zero,
+                      sem_solver_results* res)
+{
+    const int nc = (op == OP_RES) ? 2 : 1;
+    KrylovWork<double> w{};
+    GridSync* sync = nullptr;
+    SolveOut* out = nullptr;
+    int s = krylov_work(c, nc, &w, &sync, &out);
+    if (s) return s;
+    int grid = 0;
+    dispatch_n(c->N, [&](auto nv) {
+        grid = solver_grid<decltype(nv)::value>(op, nc, c->sms);
+        return cudaSuccess;
+    });
+    if (grid <= 0) return fail(SEM_ERR_CUDA, "could not size the cooperative grid");
+    const int chunks = (c->E + 0) / 1;  // one block needs at least one element
+    grid = std::min(grid, std::max(1, chunks));
+    grid = std::min(grid, 152 * 64);
+    SolveArgs a{};
+    a.op = op;
+    a.nc = nc;
+    a.pot = pot;
+    a.alpha = alpha;
+    a.b[0] = b[0];
+    a.b[1] = nc == 2 ? b[1] : nullptr;
+    a.x[0] = x[0];
+    a.x[1] = nc == 2 ? x[1] : nullptr;
+    a.maxit = maxit;
+    a.tol = tol;
+    a.x_is_zero = x_is_zero;
+    a.timeout_ns = (long long)(c->timeout_ms * 1e6);
+    a.sync = sync;
+    a.out = out;
+    SEM_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), c->stream));
+    SEM_CUDA(cudaMemsetAsync(out, 0, sizeof(SolveOut), c->stream));
+    cudaError_t e;
+    if (op == OP_LAPLACE)
+        e = dispatch_n(c->N, [&](auto nv) { return launch_pcg<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
+    else
+        e = dispatch_n(c->N, [&](auto nv) { return launch_minres<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
+    if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
+    SEM_CUDA(cudaMemcpyAsync(c->h_out, out, sizeof(SolveOut), cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(c->h_sync, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->h_sync->err) return fail(SEM_ERR_DEVICE_WAIT, "a grid barrier timed out");
+    res->success = c->h_out->success;
+    res->n_iter = c->h_out->n_iter;
+    res->residual = c->h_out->residual;
+    c->stats.krylov_iterations += res->n_iter;
+    c->stats.fp64_applies += res->n_iter + 1 + (x_is_zero ? 0 : 1);
+    return SEM_OK;
+}
+
+extern "C" int sem_minres_schro(sem_ctx* c, const double* V, double alpha, double* xr, double* xi,
+                                const double* br, const double* bi, int maxit, double tol,
+                                int x_is_zero, sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!V || !xr || !xi || !br || !bi || !res) return fail(SEM_ERR_ARG, "null argument");
+    double* x[2] = {xr, xi};
+    const double* b[2] = {br, bi};
+    return run_krylov(c, OP_RES, V, alpha, x, b, maxit, tol, x_is_zero, res);
+}
+
+extern "C" int sem_minres_helmholtz(sem_ctx* c, const double* cf, double* x, const double* b,
+                                    int maxit, double tol, int x_is_zero, sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!cf || !x || !b || !res) return fail(SEM_ERR_ARG, "null argument");
+    double* xx[2] = {x, nullptr};
+    const double* bb[2] = {b, nullptr};
+    return run_krylov(c, OP_HELM, cf, 0.0, xx, bb, maxit, tol, x_is_zero, res);
+}
+
+extern "C" int sem_pcg_laplace(sem_ctx* c, double* x, const double* b, int max_iter, double tol,
+                               int x_is_zero, sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!x || !b || !res) return fail(SEM_ERR_ARG, "null argument");
+    double* xx[2] = {x, nullptr};
+    const double* bb[2] = {b, nullptr};
+    return run_krylov(c, OP_LAPLACE, nullptr, 0.0, xx, bb, max_iter, tol, x_is_zero, res);
+}
+
+// ------------------------------------------------------------ C ABI: drivers
+// stage a caller field on the device: returns a device pointer (the caller's
+// own when it already is one)
+static int stage_in(sem_ctx* c, const char* name, const double* src, size_t count, const double** out,
+                    bool* was_host)
+{
+    *was_host = !is_device_ptr(src);
+    if (!*was_host) {
+        *out = src;
+        return SEM_OK;
+    }
+    double* d = nullptr;
+    int s = wsget(c, name, count, &d);
+    if (s) return s;
+    SEM_CUDA(cudaMemcpyAsync(d, src, sizeof(double) * count, cudaMemcpyHostToDevice, c->stream));
+    *out = d;
+    return SEM_OK;
+}
+
+extern "C" int sem_poisson(sem_ctx* c, double* u, const double* f, int max_iter, double tol,
+                           sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!u || !f || !res) return fail(SEM_ERR_ARG, "null argument");
+    bool uh = false, fh = false;
+    const double* fd = nullptr;
+    const double* ud0 = nullptr;
+    int s = 0;
+    if ((s = stage_in(c, "drv_f", f, c->n, &fd, &fh))) return s;
+    if ((s = stage_in(c, "drv_u", u, c->n, &ud0, &uh))) return s;
+    double* ud = const_cast<double*>(ud0);
+    double* b = nullptr;
+    if ((s = wsget(c, "drv_b", c->n, &b))) return s;
+    if ((s = sem_gproj(c, fd, b))) return s;  // poisson.hpp:20
+    if ((s = sem_pcg_laplace(c, ud, b, max_iter, tol, 0, res))) return s;
+    if (uh) {
+        SEM_CUDA(cudaMemcpyAsync(u, ud, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
+        SEM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return SEM_OK;
+}
+
+extern "C" int sem_helmholtz(sem_ctx* c, double* u, const double* cf, const double* f, int max_iter,
+                             double tol, sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!u || !cf || !f || !res) return fail(SEM_ERR_ARG, "null argument");
+    bool uh = false, fh = false, ch = false;
+    const double *fd = nullptr, *cd = nullptr, *ud0 = nullptr;
+    int s = 0;
+    if ((s = stage_in(c, "drv_f", f, c->n, &fd, &fh))) return s;
+    if ((s = stage_in(c, "drv_c", cf, c->n, &cd, &ch))) return s;
+    if ((s = stage_in(c, "drv_u", u, c->n, &ud0, &uh))) return s;
+    double* ud = const_cast<double*>(ud0);
+    double* b = nullptr;
+    if ((s = wsget(c, "drv_b", c->n, &b))) return s;
+    if ((s = sem_gproj(c, fd, b))) return s;  // helmholtz.hpp:21
+    if ((s = sem_minres_helmholtz(c, cd, ud, b, max_iter, tol, 0, res))) return s;
+    if (uh) {
+        SEM_CUDA(cudaMemcpyAsync(u, ud, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
+        SEM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return SEM_OK;
+}
+
+// state shared by the three Schroedinger drivers
+struct SchroRun {
+    sem_ctx* c;
+    double* psi_re;
+    double* psi_im;
+    bool host;
+    const double* V;  // device
+    double* P[2];     // two-plane state ping-pong
+    int cur;
+    long long n;
+};
+
+static int schro_begin(sem_ctx* c, double* psi_re, double* psi_im, const double* V, SchroRun* r)
+{
+    r->c = c;
+    r->psi_re = psi_re;
+    r->psi_im = psi_im;
+    r->n = c->n;
+    r->cur = 0;
+    r->host = !is_device_ptr(psi_re);
+    bool vh = false;
+    int s = 0;
+    if ((s = stage_in(c, "drv_V", V, c->n, &r->V, &vh))) return s;
+    if ((s = wsget(c, "drv_P0", 2 * c->n, &r->P[0]))) return s;
+    if ((s = wsget(c, "drv_P1", 2 * c->n, &r->P[1]))) return s;
+    const cudaMemcpyKind k = r->host ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    SEM_CUDA(cudaMemcpyAsync(r->P[0], psi_re, sizeof(double) * c->n, k, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(r->P[0] + c->n, psi_im, sizeof(double) * c->n, k, c->stream));
+    c->stats.steps_taken = 0;
+    return SEM_OK;
+}
+
+static int schro_publish(SchroRun* r)
+{
+    sem_ctx* c = r->c;
+    const cudaMemcpyKind k = r->host ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+    SEM_CUDA(cudaMemcpyAsync(r->psi_re, r->P[r->cur], sizeof(double) * c->n, k, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(r->psi_im, r->P[r->cur] + c->n, sizeof(double) * c->n, k, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    return SEM_OK;
+}
+
+// b = dt * f(p + sum a_l z_l), masked (schrodinger.hpp:221,229,378,386)
+static int schro_rhs(SchroRun* r, double dt, const ZList& zl, double* b)
+{
+    sem_ctx* c = r->c;
+    double* Y = nullptr;
+    int s = wsget(c, "apply_Y", 2 * c->n, &Y);
+    if (s) return s;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_combo_f<decltype(nv)::value>(c->dm, r->V, r->P[r->cur], zl, Y, c->stream);
+    }));
+    for (int q = 0; q < 2; ++q)
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_dss<decltype(nv)::value>(c->dm, false, DSS_MASK, dt, Y + q * c->n, b + q * c->n, c->stream);
+        }));
+    c->stats.fp64_applies++;
+    return SEM_OK;
+}
+
+static int schro_stage_solve(SchroRun* r, double alpha, const double* b, double* z, int max_iter,
+                             double tol, int x_is_zero, sem_solver_results* res)
+{
+    sem_ctx* c = r->c;
+    double* x[2] = {z, z + c->n};
+    const double* bb[2] = {b, b + c->n};
+    return run_krylov(c, OP_RES, r->V, alpha, x, bb, max_iter, tol, x_is_zero, res);
+}
+
+static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, const double* V,
+                       double T, const sem_solver_opts* o, sem_step_callback cb, void* user,
+                       int* success)
+{
+    SEM_CHECK_CTX(c);
+    if (!psi_re || !psi_im || !V || !o || !success) return fail(SEM_ERR_ARG, "null argument");
+    SchroRun r{};
+    int s = schro_begin(c, psi_re, psi_im, V, &r);
+    if (s) return s;
+    double alpha;
+    std::vector<std::vector<double>> arow;
+    std::vector<double> bw, ew;
+    if (stages == 3) {
+        // schrodinger.hpp:297-301, 385, 393, 401
+        const double gamma = std::cos(M_PI / 18.0) / std::sqrt(3.0) + 0.5;
+        const double delta = 1.0 / 6.0 / std::pow(2 * gamma - 1, 2);
+        alpha = gamma * o->dt;
+        arow = {{}, {0.5 - gamma}, {2 * gamma, 1 - 4 * gamma}};
+        bw = {delta, 1 - 2 * delta, delta};
+    } else {
+        // schrodinger.hpp:142, 228-262 (Hairer-Wanner SDIRK4, 5 stages)
+        alpha = 0.25 * o->dt;
+        arow = {{},
+                {0.5},
+                {17.0 / 50.0, -1.0 / 25.0},
+                {371.0 / 1360.0, -137.0 / 2720.0, 15.0 / 544.0},
+                {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0}};
+        bw = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0, 0.25};
+        ew = {-3.0 / 16.0, -27.0 / 32.0, 25.0 / 32.0, 0.0, 0.25};
+    }
+    double* Z = nullptr;
+    double* b = nullptr;
+    if ((s = wsget(c, "drv_Z", (size_t)stages * 2 * c->n, &Z))) return s;
+    if ((s = wsget(c, "drv_b2", 2 * c->n, &b))) return s;
+    double pnorm = 0.0;
+    if (stages == 5) {
+        double a1 = 0, a2 = 0;
+        if ((s = dot_dev(c, r.P[0], r.P[0], &a1)) || (s = dot_dev(c, r.P[0] + c->n, r.P[0] + c->n, &a2))) return s;
+        pnorm = std::sqrt(a1 + a2);  // schrodinger.hpp:214
+    }
+    bool ok = true;
+    double t = 0.0;
+    int step = 0;
+    while (t < T) {  // schrodinger.hpp:219, 376
+        c->stats.last_step_stages = stages;
+        for (int st = 0; st < stages; ++st) {
+            ZList zl{};
+            zl.nz = st;
+            for (int l = 0; l < st; ++l) {
+                zl.z[l] = Z + (size_t)l * 2 * c->n;
+                zl.c[l] = arow[st][l];
+            }
+            if ((s = schro_rhs(&r, o->dt, zl, b))) return s;
+            double* z = Z + (size_t)st * 2 * c->n;
+            SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
+            sem_solver_results res{};
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, 1, &res))) return s;
+            c->stats.last_stage_iters[st] = res.n_iter;
+            c->stats.last_stage_sweeps[st] = 1;
+            if (!res.success) {
+                ok = false;
+                break;
+            }
+        }
+        if (!ok) break;
+        ZList zb{};
+        zb.nz = stages;
+        for (int l = 0; l < stages; ++l) {
+            zb.z[l] = Z + (size_t)l * 2 * c->n;
+            zb.c[l] = bw[l];
+        }
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_update<decltype(nv)::value>(c->dm, r.P[r.cur], zb, r.P[1 - r.cur], c->stream);
+        }));
+        r.cur = 1 - r.cur;
+        if (stages == 5) {  // embedded error estimate (schrodinger.hpp:262-263)
+            double* err = nullptr;
+            if ((s = wsget(c, "drv_err", 2 * c->n, &err))) return s;
+            ZList ze{};
+            ze.nz = 0;
+            for (int l = 0; l < 5; ++l)
+                if (ew[l] != 0.0) {
+                    ze.z[ze.nz] = Z + (size_t)l * 2 * c->n;
+                    ze.c[ze.nz++] = ew[l];
+                }
+            k_lincomb<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, ze, err);
+            SEM_CUDA(cudaGetLastError());
+            double a1 = 0, a2 = 0;
+            if ((s = dot_dev(c, err, err, &a1)) || (s = dot_dev(c, err + c->n, err + c->n, &a2))) return s;
+            c->stats.last_error_estimate = std::sqrt(a1 + a2) / pnorm;
+        }
+        t += o->dt;
+        ++step;
+        c->stats.steps_taken = step;
+        if (cb) {
+            if ((s = schro_publish(&r))) return s;
+            if (cb(user, step, psi_re, psi_im)) break;
+        }
+    }
+    if ((s = schro_publish(&r))) return s;
+    *success = ok ? 1 : 0;
+    return SEM_OK;
+}
+
+extern "C" int sem_schrodinger_dirk4s3(sem_ctx* c, double* psi_re, double* psi_im, const double* V,
+                                       double T, const sem_solver_opts* o, sem_step_callback cb,
+                                       void* user, int* success)
+{
+    return schro_sdirk(c, 3, psi_re, psi_im, V, T, o, cb, user, success);
+}
+
+extern "C" int sem_schrodinger_dirk4s5(sem_ctx* c, double* psi_re, double* psi_im, const double* V,
+                                       double T, const sem_solver_opts* o, sem_step_callback cb,
+                                       void* user, int* success)
+{
+    return schro_sdirk(c, 5, psi_re, psi_im, V, T, o, cb, user, success);
+}
+
+extern "C" int sem_schrodinger_bdf2(sem_ctx* c, double* psi_re, double* psi_im, const double* V,
+                                    double T, const sem_solver_opts* o, sem_step_callback cb,
+                                    void* user, int* success)
+{
+    SEM_CHECK_CTX(c);
+    if (!psi_re || !psi_im || !V || !o || !success) return fail(SEM_ERR_ARG, "null argument");
+    SchroRun r{};
+    int s = schro_begin(c, psi_re, psi_im, V, &r);
+    if (s) return s;
+    double* PS[2] = {nullptr, nullptr};
+    double* b = nullptr;
+    if ((s = wsget(c, "drv_PS0", 2 * c->n, &PS[0])) || (s = wsget(c, "drv_PS1", 2 * c->n, &PS[1])) ||
+        (s = wsget(c, "drv_b2", 2 * c->n, &b)))
+        return s;
+    double alpha = o->dt;  // schrodinger.hpp:26
+    int nps = 0;
+    bool ok = true;
+    double t = 0.0;
+    int step = 0;
+    double* p = r.P[0];
+    while (t < T) {  // schrodinger.hpp:89
+        if (nps == 2) {
+            std::swap(PS[0], PS[1]);
+            nps = 1;
+        }
+        double* dst = PS[nps];
+        // proj(p) = [gproj(re); -gproj(im)] (schrodinger.hpp:69-78)
+        if ((s = apply_galerkin(c, OP_MASS, nullptr, 0.0, p, nullptr, dst, nullptr, 1.0))) return s;
+        if ((s = apply_galerkin(c, OP_MASS, nullptr, 0.0, p + c->n, nullptr, dst + c->n, nullptr, -1.0))) return s;
+        ++nps;
+        sem_solver_results res{};
+        double* x[2] = {p, p + c->n};
+        c->stats.last_step_stages = 1;
+        if (nps == 1) {
+            const double* bb[2] = {PS[0], PS[0] + c->n};
+            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res))) return s;
+            alpha = (2.0 / 3.0) * o->dt;
+        } else {
+            k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, -1.0 / 3.0, PS[0], 4.0 / 3.0, PS[1], b);
+            SEM_CUDA(cudaGetLastError());
+            const double* bb[2] = {b, b + c->n};
+            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res))) return s;
+        }
+        c->stats.last_stage_iters[0] = res.n_iter;
+        c->stats.last_stage_sweeps[0] = 1;
+        if ((s = sem_unmask(c, p)) || (s = sem_unmask(c, p + c->n))) return s;
+        t += o->dt;
+        if (!res.success) {
+            ok = false;
+            break;
+        }
+        ++step;
+        c->stats.steps_taken = step;
+        if (cb) {
+            if ((s = schro_publish(&r))) return s;
+            if (cb(user, step, psi_re, psi_im)) break;
+        }
+    }
+    if ((s = schro_publish(&r))) return s;
+    *success = ok ? 1 : 0;
+    return SEM_OK;
+}

@@ -1,0 +1,5 @@
+// Explicit instantiations of the kernel launchers for N = 16 17 (p = N-1).
+// The degrees are split over several units so they compile in parallel.
+#include "sem_kernels.cuh"
+SEM_INSTANTIATE(16)
+SEM_INSTANTIATE(17)

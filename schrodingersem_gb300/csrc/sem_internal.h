@@ -1,0 +1,141 @@
+// Internal declarations shared by the host side (sem_host.cu) and the
+// per-degree kernel instantiation units (sem_inst.cu).  Not installed.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+namespace semgb {
+
+constexpr int MIN_N = 2;   // p = 1
+constexpr int MAX_N = 17;  // p = 16
+
+// Element-local operator kinds (the closures of the reference's drivers).
+enum OpKind : int {
+    OP_LAPLACE = 0,  // glaplace                         (glaplace.hpp:16-28)
+    OP_HELM = 1,     // glaplace + (W (u%c) W) % J      (helmholtz.hpp:44-45)
+    OP_MASS = 2,     // (W u W) % J                      (galerkin.hpp:51)
+    OP_RES = 3,      // [M u + a L v ; a L u - M v]      (schrodinger.hpp:353-360)
+    OP_F = 4         // [-L v ; -L u]                    (schrodinger.hpp:331-336)
+};
+
+// Assembly modes of the direct-stiffness sum.
+enum DssMode : int {
+    DSS_SUM = 0,   // global_sum: shared interior nodes get the sum at every copy, boundary untouched
+    DSS_MASK = 1,  // global_sum then mask: sum at the owner copy, zero elsewhere and on the boundary
+    DSS_CONT = 2   // sum at every copy, zero on the boundary (the solvers' continuous format)
+};
+
+// Per-element topology bits in DevMesh::flags.
+//  bits 0-3   side s owned by this element (it is Edge::elements[0])
+//  bits 4-7   side s on the boundary
+//  bits 8-11  corner c owned (first of CornerNode::connected_elements)
+//  bits 12-15 corner c on the boundary
+// Sides s = 0..3 are the reference's sides 1..4: j=0, i=N-1, j=N-1, i=0.
+// Corners c = 0..3 are (0,0), (N-1,0), (N-1,N-1), (0,N-1).
+
+struct DevMesh {
+    int N = 0, E = 0, n_nodes = 0;
+    long long n = 0;  // E*N*N
+    const int* flags = nullptr;
+    const int* side_base = nullptr;  // [E*4] neighbour flat index at k = 0 (valid for interior sides)
+    const int* side_step = nullptr;  // [E*4] neighbour flat-index step per k
+    const int* corner_src = nullptr; // [E*4] flat index of the corner's owner copy
+    const int* corner_node = nullptr;// [E*4] corner node id
+    const int* node_ptr = nullptr;   // [n_nodes+1] CSR over copies of each corner node
+    const int* node_flat = nullptr;  // flat indices of the copies, element order
+    const double* D64 = nullptr;     // D row-major: D(i,k) at [i*N+k]
+    const float* D32 = nullptr;
+    // premultiplied factors w_i w_j {A, B, C, J}
+    const double *g11 = nullptr, *g12 = nullptr, *g22 = nullptr, *mass = nullptr;
+    const float *g11f = nullptr, *g12f = nullptr, *g22f = nullptr, *massf = nullptr;
+};
+
+// Grid barrier and error state of a persistent (cooperative) kernel.
+struct GridSync {
+    unsigned int count;
+    unsigned int gen;
+    int err;   // nonzero: a wait hit its limit
+    int pad;
+};
+
+// Device-side result of a persistent solve.
+struct SolveOut {
+    int success;
+    int n_iter;
+    double residual;
+    int status;      // 0 or SEM_ERR_DEVICE_WAIT
+    int inner_iters; // mixed mode: total FP32 iterations
+    int sweeps;      // mixed mode: refinement sweeps
+    int pad;
+};
+
+template <typename T>
+struct KrylovWork {
+    T* L[3];        // Lanczos vectors (NC planes each)
+    T* W[3];        // MINRES direction vectors / PCG p, r
+    T* Y[2];        // element-local operator output
+    double* partials;  // [2 slots][grid][4]
+};
+
+struct SolveArgs {
+    int op;          // OP_RES, OP_HELM, OP_LAPLACE
+    int nc;          // 1 or 2 planes
+    const void* pot; // V or c field (same precision as T), may be null for LAPLACE
+    double alpha;
+    const void* b[2]; // right-hand side planes (masked format)
+    void* x[2];       // solution planes, in/out
+    int maxit;
+    double tol;
+    int x_is_zero;
+    long long timeout_ns;
+    GridSync* sync;
+    SolveOut* out;
+};
+
+// ---- launchers, one explicit instantiation per N in sem_inst.cu -------------
+template <int N>
+cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, double alpha,
+                         const void* in0, const void* in1, void* y0, void* y1, bool gather,
+                         cudaStream_t st);
+template <int N>
+cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
+                       void* out, cudaStream_t st);
+template <int N>
+cudaError_t launch_unmask(const DevMesh& m, bool fp32, void* a, cudaStream_t st);
+template <int N>
+cudaError_t launch_mask(const DevMesh& m, bool fp32, void* a, cudaStream_t st);
+// weighted dot: partial sums per block into part[grid], returns grid used
+template <int N>
+cudaError_t launch_dot(const DevMesh& m, const double* a, const double* b, double* part,
+                       int max_blocks, int* blocks_used, cudaStream_t st);
+// out[n] = gather(p + sum_l c[l] z_l) for every node (unmask semantics); then
+// optional f-apply: y = L-closure of the combination.
+struct ZList {
+    int nz;
+    const double* z[8];  // two-plane vectors (plane stride n)
+    double c[8];
+};
+template <int N>
+cudaError_t launch_combo_f(const DevMesh& m, const double* V, const double* p, const ZList& zl,
+                           double* y, cudaStream_t st);
+// p_out = unmask(p_in + sum_l c[l] z_l), both planes
+template <int N>
+cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl, double* p_out,
+                          cudaStream_t st);
+// persistent Krylov solvers (cooperative launch)
+template <int N>
+cudaError_t launch_minres(const DevMesh& m, const SolveArgs& a, const KrylovWork<double>& w,
+                          int grid, cudaStream_t st);
+template <int N>
+cudaError_t launch_pcg(const DevMesh& m, const SolveArgs& a, const KrylovWork<double>& w,
+                       int grid, cudaStream_t st);
+// co-resident grid size for the persistent solvers
+template <int N>
+int solver_grid(int op, int nc, int sms);
+
+}  // namespace semgb
+
+#define SEM_FOR_EACH_N(X) \
+    X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)

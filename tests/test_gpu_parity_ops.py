@@ -1,0 +1,133 @@
+"""Parity of the CUDA operators with the CPU oracle, through the C ABI.
+
+Gather-scatter (unmask, global_sum, mask) is compared bit for bit; the
+operator applies within 1e-12 relative in FP64 (the tolerance the hot path
+is specified to), the FP32 apply within 2e-5 relative."""
+import numpy as np
+import pytest
+
+from tests.util import SMALL_MESH, rel_err, structured
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+TOL32 = 2e-5
+
+
+def _pair(semlib, oracle, p, kind, corrected=False):
+    if kind == "small":
+        ctx = semlib.Context(p, folder=SMALL_MESH, corrected_metric=corrected)
+        om = oracle.Mesh(p, folder=SMALL_MESH, ref_compat=not corrected)
+    else:
+        co, el = structured(5 if p < 10 else 3, box=(-1.0, 2.0, -0.5, 1.5), jitter=0.2, seed=p)
+        ctx = semlib.Context(p, coords=co, elements=el, corrected_metric=corrected)
+        om = oracle.Mesh(p, coords=co, elements=el, ref_compat=not corrected)
+    return ctx, om
+
+
+CASES = [("small", p) for p in (1, 2, 3, 6, 8)] + [("jit", p) for p in range(1, 17)]
+
+
+@pytest.mark.parametrize("kind,p", CASES)
+def test_setup_matches(semlib, oracle, kind, p):
+    ctx, om = _pair(semlib, oracle, p, kind)
+    x, w, D = ctx.quadrature()
+    tol = 0 if p <= 8 else 2e-15
+    assert np.max(abs(x - om.x)) <= tol
+    assert np.max(abs(w - om.w)) <= (0 if p <= 8 else 1e-14)
+    assert np.max(abs(D - om.D)) <= (0 if p <= 8 else 1e-11 * np.max(abs(om.D)))
+    J, A, B, C = ctx.metrics()
+    for a, b in ((J, om.J), (A, om.A), (B, om.B), (C, om.C)):
+        assert rel_err(a, b) <= (0 if p <= 8 else 1e-14)
+    assert ctx.dof() == om.dof()
+    X, Y = ctx.node_coords()
+    OX, OY = om.node_coords()
+    assert np.max(abs(X - OX)) <= 1e-15 * 4 and np.max(abs(Y - OY)) <= 1e-15 * 4
+
+
+@pytest.mark.parametrize("kind,p", CASES)
+def test_gather_scatter_bit_exact(semlib, oracle, kind, p):
+    ctx, om = _pair(semlib, oracle, p, kind)
+    rng = np.random.default_rng(100 + p)
+    a = rng.standard_normal(om.shape)
+    for name in ("unmask", "global_sum", "mask"):
+        d = ctx.to_device(a)
+        getattr(ctx, name)(d)
+        got = d.cpu().numpy()
+        want = getattr(om, name)(a)
+        assert np.array_equal(got, want), name
+    b = rng.standard_normal(om.shape)
+    got = ctx.dot(ctx.to_device(a), ctx.to_device(b))
+    want = om.dot(a, b)
+    assert abs(got - want) <= 1e-13 * (abs(want) + np.sqrt(om.dot(a, a) * om.dot(b, b)))
+    one = ctx.to_device(np.ones(om.shape))
+    assert ctx.dot(one, one) == om.dof()  # mpi_tests/dot.cpp:9-33
+
+
+@pytest.mark.parametrize("kind,p", CASES)
+@pytest.mark.parametrize("corrected", [False, True])
+def test_operators_fp64(semlib, oracle, kind, p, corrected):
+    ctx, om = _pair(semlib, oracle, p, kind, corrected)
+    rng = np.random.default_rng(7 * p + 3)
+    u = rng.standard_normal(om.shape)
+    v = rng.standard_normal(om.shape)
+    V = rng.uniform(-5, 5, om.shape)
+    du, dv, dV = ctx.to_device(u), ctx.to_device(v), ctx.to_device(V)
+    assert rel_err(ctx.gproj(du).cpu().numpy(), om.gproj(u)) <= TOL64
+    assert rel_err(ctx.apply_laplace(du).cpu().numpy(), om.apply_laplace(u)) <= TOL64
+    assert rel_err(ctx.apply_helmholtz(dV, du).cpu().numpy(), om.apply_helmholtz(V, u)) <= TOL64
+    alpha = 0.0123
+    yr, yi = ctx.schro_res(dV, alpha, du, dv)
+    orr, oii = om.schro_res(V, alpha, u, v)
+    assert rel_err(yr.cpu().numpy(), orr) <= TOL64 and rel_err(yi.cpu().numpy(), oii) <= TOL64
+    yr, yi = ctx.schro_f(dV, du, dv)
+    orr, oii = om.schro_f(V, u, v)
+    assert rel_err(yr.cpu().numpy(), orr) <= TOL64 and rel_err(yi.cpu().numpy(), oii) <= TOL64
+    # outputs are masked: applying mask again changes nothing
+    out = ctx.apply_laplace(du)
+    again = out.clone()
+    ctx.mask(again)
+    assert bool((again == out).all())
+
+
+@pytest.mark.parametrize("kind,p", [("small", 3), ("small", 8), ("jit", 4), ("jit", 8), ("jit", 12), ("jit", 16)])
+def test_schro_res_fp32(semlib, oracle, kind, p):
+    import torch
+    ctx, om = _pair(semlib, oracle, p, kind)
+    rng = np.random.default_rng(p)
+    u, v = rng.standard_normal(om.shape), rng.standard_normal(om.shape)
+    V = rng.uniform(-5, 5, om.shape)
+    f = torch.float32
+    yr, yi = ctx.schro_res_f32(ctx.to_device(V, f), 0.05, ctx.to_device(u, f), ctx.to_device(v, f))
+    orr, oii = om.schro_res(V.astype(np.float32).astype(np.float64), 0.05,
+                            u.astype(np.float32).astype(np.float64), v.astype(np.float32).astype(np.float64))
+    assert rel_err(yr.cpu().double().numpy(), orr) <= TOL32
+    assert rel_err(yi.cpu().double().numpy(), oii) <= TOL32
+
+
+def test_apply_unmasked_input_uses_owner_copies(semlib, oracle):
+    # galerkin_op unmasks its input: non-owner copies of shared nodes are
+    # ignored, boundary copies are used as given (galerkin.hpp:24-35)
+    ctx, om = _pair(semlib, oracle, 4, "small")
+    rng = np.random.default_rng(5)
+    u = rng.standard_normal(om.shape)
+    junk = u.copy()
+    shared_non_owner = (om.unmask(om.mask(np.ones(om.shape))) == 1) & (om.mask(np.ones(om.shape)) == 0)
+    junk[shared_non_owner] = 1e3
+    a = ctx.apply_laplace(ctx.to_device(u)).cpu().numpy()
+    b = ctx.apply_laplace(ctx.to_device(junk)).cpu().numpy()
+    assert rel_err(a, om.apply_laplace(u)) <= TOL64
+    assert rel_err(b, om.apply_laplace(junk)) <= TOL64
+    assert np.array_equal(b, ctx.apply_laplace(ctx.to_device(om.unmask(junk))).cpu().numpy())
+
+
+def test_vec_axpby(semlib):
+    import torch
+    co, el = structured(3)
+    ctx = semlib.Context(2, coords=co, elements=el)
+    x = torch.randn(ctx.shape, dtype=torch.float64, device="cuda")
+    y = torch.randn(ctx.shape, dtype=torch.float64, device="cuda")
+    out = torch.empty_like(x)
+    ctx.axpby(2.0, x, -0.5, y, out)
+    torch.cuda.synchronize()
+    assert torch.allclose(out, 2.0 * x + (-0.5) * y, rtol=1e-15, atol=1e-15)
