@@ -1,0 +1,388 @@
+#!/usr/bin/env python3
+"""Benchmark: seconds per Schroedinger time step on one GB300.
+
+Workload (the configuration the headline metric is quoted on): SDIRK4
+3-stage on 64x64 bilinear quads over [-8,8]^2, interior vertices jittered by
++-0.1h (seed 1), p = 8 (513^2 = 263,169 global nodes, 331,776 element-local
+nodes per component), V = (x^2+y^2)/2, normalised Gaussian packet (sigma 1,
+centre (-2,0), momentum (3,0)), dt = 1e-2, MINRES tolerance 1e-10.  The
+reference solves i psi_t = -(-lap + V) psi; the workload's
+i psi_t = -lap/2 psi + V psi maps onto it exactly with V' = 2V, dt' = dt/2 and
+psi' = conj(psi).
+
+A step is one time step (3 implicit stages).  ``value`` is the device-time
+of a step with the state resident in HBM (L2 flushed before every step);
+``e2e`` is the same step through the C ABI with host (pinned) buffers, the
+host<->device copies inside the timed region.  ``--impl reference`` times
+the CPU oracle (a restatement of the reference's OpenMP path; the reference
+itself cannot be built here) on the host cores on the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "s/time-step at 1e-8 rel err vs FP64: learned+FP32 vs plain GPU; apply GB/s"
+WORKLOAD = ("Schroedinger SDIRK4-3 time step, 64x64 jittered quads on [-8,8]^2 (seed 1), p=8 "
+            "(263,169 nodes), V=(x^2+y^2)/2, Gaussian packet sigma=1 r0=(-2,0) k=(3,0), dt=1e-2, "
+            "MINRES tol 1e-10")
+DT, TOL, P, NEL = 1e-2, 1e-10, 8, 64
+
+
+def workload_inputs():
+    """mesh + reference-convention inputs (V' = 2V, dt' = dt/2, psi' = conj psi)"""
+    from schrodingersem_gb300.meshgen import element_node_coords, gaussian_packet, structured_quads
+    co, el = structured_quads(NEL, box=(-8.0, 8.0, -8.0, 8.0), jitter=0.1, seed=1)
+    return co, el
+
+
+def fields(ctx_or_mesh):
+    X, Y = ctx_or_mesh.node_coords()
+    from schrodingersem_gb300.meshgen import gaussian_packet
+    re, im = gaussian_packet(X, Y, (-2.0, 0.0), 1.0, (3.0, 0.0))
+    return X, Y, re, im
+
+
+def mass_norm(J, w, re, im):
+    ww = w[None, :, None] * w[None, None, :]
+    return math.sqrt(float(np.sum(ww * J * (re * re + im * im))))
+
+
+def flush_l2(buf):
+    buf.zero_()
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region"""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.index), "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [t.strip() for t in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- reference
+def run_reference(args):
+    """CPU oracle (restatement of the reference's OpenMP path) on host cores."""
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    co, el = workload_inputs()
+    om = O.Mesh(P, coords=co, elements=el)
+    X, Y, re, im = fields(om)
+    nrm = mass_norm(om.J, om.w, re, im)
+    re, im = re / nrm, im / nrm
+    Vr = 2.0 * 0.5 * (X * X + Y * Y)
+    dtr = DT / 2.0
+    # a full CPU step of this workload takes tens of seconds, so the run is
+    # bounded: at most one warm-up step, then timed steps until the budget
+    # is spent (at least one)
+    budget_s = float(os.environ.get("SEM_REF_BUDGET_S", "150"))
+    warm = min(args.warmup, 1)
+    total = warm + args.steps
+    times = []
+    t_last = [0.0]
+    import ctypes as C
+
+    def _cb(user, step, a, b, iters, n):
+        now = time.perf_counter()
+        times.append(now - t_last[0])
+        t_last[0] = now
+        if step >= total:
+            return 1
+        if step > warm and sum(times[warm:]) > budget_s:
+            return 1
+        return 0
+
+    cbf = O._CB(_cb)
+    pr, pi = np.ascontiguousarray(re), np.ascontiguousarray(-im)
+    V = np.ascontiguousarray(Vr)
+    opts = O.OrOpts(20 * om.dof(), TOL, dtr, 0)
+    t_last[0] = time.perf_counter()
+    O.lib().or_schrodinger_dirk4s3(om._ptr, O._p(pr), O._p(pi), O._p(V), 1e9, C.byref(opts), cbf, None)
+    timed = times[warm:] if len(times) > warm else times[-1:]
+    sps = float(np.mean(timed))
+    line = {"impl": "reference", "metric": METRIC, "value": sps, "unit": "s/step", "n_gpus": args.gpus,
+            "steps": len(timed), "warmup": warm,
+            "ms_per_step": sps * 1e3, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "form": "reference OpenMP path (CPU oracle port)"},
+            "cpu_baseline": {"value": sps, "unit": "s/step", "cores": threads, "kind": "port",
+                             "sample": f"{len(timed)} timed SDIRK4-3 steps after {args.warmup} warm-up, "
+                                       f"OpenMP {threads} threads"},
+            "e2e": {"value": sps, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ----------------------------------------------------------------- ours
+def cpu_baseline_sample(iters_per_step, cap=60):
+    """Bounded CPU sample: the oracle's first-stage MINRES of the workload,
+    capped at `cap` iterations (plus its right-hand side), after one untimed
+    repetition; scaled to a step by the step's measured MINRES iteration
+    total (the GPU runs the same algorithm, so the counts agree)."""
+    import ctypes as C
+
+    from oracle import oracle as O
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    co, el = workload_inputs()
+    om = O.Mesh(P, coords=co, elements=el)
+    X, Y, re, im = fields(om)
+    nrm = mass_norm(om.J, om.w, re, im)
+    V = np.ascontiguousarray(X * X + Y * Y)
+    opts = O.OrOpts(int(cap), TOL, DT / 2, 0)
+    secs = []
+    for _ in range(2):
+        pr, pi = np.ascontiguousarray(re / nrm), np.ascontiguousarray(-im / nrm)
+        t0 = time.perf_counter()
+        O.lib().or_schrodinger_dirk4s3(om._ptr, O._p(pr), O._p(pi), O._p(V), 1e9, C.byref(opts),
+                                       O._CB(0), None)
+        secs.append(time.perf_counter() - t0)
+    per_iter = secs[-1] / cap
+    return {"value": per_iter * iters_per_step, "unit": "s/step", "cores": threads, "kind": "port",
+            "sample": f"CPU oracle, OpenMP {threads} threads: first-stage MINRES of the workload capped at "
+                      f"{cap} iterations ({secs[-1]:.2f} s, after one untimed repetition), scaled by the "
+                      f"step's measured {iters_per_step:.0f} MINRES iterations"}
+
+
+def apply_gbs(ctx, torch, reps=20):
+    """standalone Res apply (element kernel + assembly) with L2 flushed before
+    each apply: algorithmic bytes n_loc * s * 9 words per apply"""
+    n = ctx.n
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    out = {}
+    for prec, dt, s in (("fp64", torch.float64, 8), ("fp32", torch.float32, 4)):
+        g = torch.Generator(device="cuda").manual_seed(0)
+        q = [torch.randn(ctx.shape, dtype=dt, device="cuda", generator=g) for _ in range(3)]
+        yr, yi = torch.empty_like(q[0]), torch.empty_like(q[0])
+        f = ctx.schro_res if prec == "fp64" else ctx.schro_res_f32
+        for _ in range(3):
+            f(q[2], 0.01, q[0], q[1], yr, yi)
+        st = torch.cuda.current_stream()
+        tot = 0.0
+        for _ in range(reps):
+            flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            f(q[2], 0.01, q[0], q[1], yr, yi)
+            e1.record(st)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        ms = tot / reps
+        bytes_ = n * s * 9
+        out[prec] = {"ms": ms, "gbs": bytes_ / ms / 1e6, "bytes": bytes_}
+    return out
+
+
+def run_ours(args):
+    import torch
+
+    import schrodingersem_gb300 as S
+    from schrodingersem_gb300 import capi
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    S.build()
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except Exception:
+        pass
+    hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    co, el = workload_inputs()
+    ctx = S.Context(P, coords=co, elements=el)
+    ctx.set_option(capi.OPT_PROFILE, 1)
+    X, Y, re, im = fields(ctx)
+    J, _, _, _ = ctx.metrics()
+    _, w, _ = ctx.quadrature()
+    nrm = mass_norm(J, w, re, im)
+    re, im = re / nrm, -im / nrm                     # psi' = conj(psi)
+    Vr = X * X + Y * Y                               # V' = 2 * (x^2+y^2)/2
+    dtr = DT / 2.0
+    maxit = 20 * ctx.dof()
+    dre, dim = ctx.to_device(re), ctx.to_device(im)
+    dV = ctx.to_device(Vr)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    st = torch.cuda.current_stream()
+
+    def one_step(pr, pi, V):
+        ok = ctx.schrodinger("dirk4s3", pr, pi, V, 0.5 * dtr, dtr, maxit, TOL)
+        if not ok:
+            raise RuntimeError("MINRES did not converge")
+
+    # warm-up
+    for _ in range(args.warmup):
+        one_step(dre, dim, dV)
+    torch.cuda.synchronize()
+    s0 = ctx.stats()
+    iters = []
+    times = []
+    with ClockSampler(local) as clk:
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        for _ in range(args.steps):
+            flush_l2(flush)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            one_step(dre, dim, dV)
+            e1.record(st)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+            sts = ctx.stats()
+            iters.append([int(sts.last_stage_iters[k]) for k in range(sts.last_step_stages)])
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+    s1 = ctx.stats()
+    ms = float(np.sum(times)) / args.steps
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    launches = int(s1.kernel_launches - s0.kernel_launches)
+    sol_ms = s1.solver_kernel_ms - s0.solver_kernel_ms
+    sol_it = s1.solver_iterations_fp64 - s0.solver_iterations_fp64
+    sol_launch = s1.solver_launches - s0.solver_launches
+
+    # e2e through the C ABI with pinned host buffers
+    h_re = torch.from_numpy(re.copy()).pin_memory()
+    h_im = torch.from_numpy(im.copy()).pin_memory()
+    h_V = torch.from_numpy(np.ascontiguousarray(Vr)).pin_memory()
+    for _ in range(min(2, args.warmup)):
+        one_step(h_re.numpy(), h_im.numpy(), h_V.numpy())
+    e2e_times = []
+    for _ in range(args.steps):
+        flush_l2(flush)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        one_step(h_re.numpy(), h_im.numpy(), h_V.numpy())
+        e1.record(st)
+        torch.cuda.synchronize()
+        e2e_times.append(e0.elapsed_time(e1))
+    e2e_s = float(np.mean(e2e_times)) / 1e3
+    nbytes = ctx.n * 8
+
+    if rank != 0:
+        return
+    app = apply_gbs(ctx, torch)
+    # MINRES iteration: one Res apply (9 words/node) + 13 two-plane vector words
+    bytes_per_iter = ctx.n * 8 * (9 + 26)
+    achieved = bytes_per_iter * sol_it / (sol_ms / 1e3) / 1e9 if sol_ms > 0 else None
+    flops_per_iter = ctx.n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
+    iters_per_step = float(np.mean([np.sum(i) for i in iters]))
+    cpu = cpu_baseline_sample(iters_per_step) if not args.no_cpu else None
+    line = {
+        "metric": METRIC, "value": ms / 1e3, "unit": "s/step", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "plain FP64 GPU MINRES (reference algorithm, zero stage guess)",
+                   "l2": "flushed before every step (256 MiB write)", "parallelism": "replicas only"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                     "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                     "kernel": "k_minres<9,double,RES> (persistent cooperative MINRES)",
+                     "bytes_per_iteration": bytes_per_iter, "iterations": sol_it,
+                     "launches": sol_launch, "kernel_ms": sol_ms, "peak_source": peak_src,
+                     "fp64_pipe": {"achieved_tflops": flops_per_iter * sol_it / (sol_ms / 1e3) / 1e12
+                                   if sol_ms > 0 else None, "peak_tflops": 1.19,
+                                   "peak_source": "FMA-chain probe on this pool's GB300"}},
+        "apply": {"fp64_gbs": app["fp64"]["gbs"], "fp32_gbs": app["fp32"]["gbs"],
+                  "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak, "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
+                  "bytes_fp64": app["fp64"]["bytes"], "note": "n_loc*s*9 words, L2 flushed before each apply"},
+        "minres_iters_per_stage": float(np.mean([np.mean(i) for i in iters])),
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e_s, "unit": "s/step", "h2d_bytes_per_step": 3 * nbytes,
+                "d2h_bytes_per_step": 2 * nbytes},
+        "clocks": clk.summary(),
+        "gpu_launches": launches,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

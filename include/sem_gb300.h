@@ -60,7 +60,8 @@ enum sem_option {
     SEM_OPT_INNER_TOL = 2,       /* relative tolerance of the FP32 inner solve (default 1e-4) */
     SEM_OPT_STAGE_GUESS = 3,     /* SEM_GUESS_ZERO (reference), _EXTRAPOLATE, _LEARNED */
     SEM_OPT_WAIT_TIMEOUT_MS = 4, /* limit of every device-side wait (default 2000 ms) */
-    SEM_OPT_MAX_REFINE = 5       /* cap on FP64 refinement sweeps in mixed mode (default 50) */
+    SEM_OPT_MAX_REFINE = 5,      /* cap on FP64 refinement sweeps in mixed mode (default 50) */
+    SEM_OPT_PROFILE = 6          /* 1: time every persistent solver launch with CUDA events */
 };
 enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
 enum { SEM_GUESS_ZERO = 0, SEM_GUESS_EXTRAPOLATE = 1, SEM_GUESS_LEARNED = 2 };
@@ -99,6 +100,11 @@ typedef struct {
     int last_stage_sweeps[8];       /* FP64 refinement sweeps per stage (1 in FP64 mode) */
     double last_error_estimate;     /* SDIRK4 5-stage embedded estimate (schrodinger.hpp:262-263) */
     int steps_taken;                /* steps of the last driver call */
+    long long kernel_launches;      /* kernels this library launched since creation */
+    long long solver_launches;      /* persistent solver launches since creation */
+    double solver_kernel_ms;        /* their summed device time (SEM_OPT_PROFILE only) */
+    long long solver_iterations_fp64; /* Krylov iterations run in FP64 */
+    long long solver_iterations_fp32; /* Krylov iterations run in FP32 */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop

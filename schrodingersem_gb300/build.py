@@ -16,8 +16,10 @@ LIBDIR = os.path.join(PKG, "_lib")
 LIB = os.path.join(LIBDIR, "libsemgb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# host code is compiled without FMA contraction so that mesh setup gives the
+# same bits on x86 and Arm hosts (and as the oracle); device code keeps fmad.
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-           "-Xcompiler", "-Wall", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
+           "-Xcompiler", "-Wall", "-Xcompiler", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
 
 def _nvcc() -> str:
@@ -37,6 +39,7 @@ def _headers():
 
 
 def _stale(target: str, deps) -> bool:
+    deps = list(deps) + [os.path.abspath(__file__)]
     if not os.path.exists(target):
         return True
     t = os.path.getmtime(target)

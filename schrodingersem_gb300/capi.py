@@ -34,7 +34,10 @@ class SemStats(C.Structure):
     _fields_ = [("krylov_iterations", C.c_longlong), ("fp64_applies", C.c_longlong),
                 ("fp32_applies", C.c_longlong), ("last_step_stages", C.c_int),
                 ("last_stage_iters", C.c_int * 8), ("last_stage_sweeps", C.c_int * 8),
-                ("last_error_estimate", C.c_double), ("steps_taken", C.c_int)]
+                ("last_error_estimate", C.c_double), ("steps_taken", C.c_int),
+                ("kernel_launches", C.c_longlong), ("solver_launches", C.c_longlong),
+                ("solver_kernel_ms", C.c_double), ("solver_iterations_fp64", C.c_longlong),
+                ("solver_iterations_fp32", C.c_longlong)]
 
 
 STEP_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, _dp, _dp)
@@ -81,7 +84,7 @@ SIGNATURES = {
 }
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
-OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE = 1, 2, 3, 4, 5
+OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
 PREC_FP64, PREC_MIXED = 0, 1
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 

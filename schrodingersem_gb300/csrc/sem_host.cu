@@ -189,6 +189,8 @@ struct sem_ctx {
     int guess = SEM_GUESS_ZERO;
     double timeout_ms = 2000.0;
     int max_refine = 50;
+    bool profile = false;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
     sem_stats stats{};
     // workspace
     std::unordered_map<std::string, DevBuf> ws;
@@ -517,6 +519,8 @@ extern "C" int sem_ctx_destroy(sem_ctx* c)
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_sync) cudaFreeHost(c->h_sync);
     if (c->h_part) cudaFreeHost(c->h_part);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
     delete c;
     return SEM_OK;
 }
@@ -568,6 +572,13 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_MAX_REFINE:
             if (!(v >= 1)) return fail(SEM_ERR_ARG, "max refine must be >= 1");
             c->max_refine = (int)v;
+            return SEM_OK;
+        case SEM_OPT_PROFILE:
+            c->profile = v != 0;
+            if (c->profile && !c->ev[0]) {
+                SEM_CUDA(cudaEventCreate(&c->ev[0]));
+                SEM_CUDA(cudaEventCreate(&c->ev[1]));
+            }
             return SEM_OK;
         default: return fail(SEM_ERR_ARG, "unknown option");
     }
@@ -628,6 +639,7 @@ extern "C" int sem_ctx_get_node_coords(const sem_ctx* c, double* X, double* Y)
     if (!(c)) return fail(SEM_ERR_ARG, "null ctx")
 #define SEM_LAUNCH(expr)                                                                       \
     do {                                                                                       \
+        c->stats.kernel_launches++;                                                            \
         cudaError_t e_ = (expr);                                                               \
         if (e_ != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("launch: ") + cudaGetErrorString(e_)); \
     } while (0)
@@ -693,6 +705,7 @@ extern "C" int sem_vec_axpby(sem_ctx* c, long long n, double a, const double* x,
     if (n < 0 || (n > 0 && (!x || !out))) return fail(SEM_ERR_ARG, "bad vector arguments");
     if (n == 0) return SEM_OK;
     k_axpby<<<grid_1d(n), 256, 0, c->stream>>>(n, a, x, b, y, out);
+    c->stats.kernel_launches++;
     SEM_CUDA(cudaGetLastError());
     return SEM_OK;
 }
@@ -837,19 +850,29 @@ static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, doubl
     SEM_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), c->stream));
     SEM_CUDA(cudaMemsetAsync(out, 0, sizeof(SolveOut), c->stream));
     cudaError_t e;
+    if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[0], c->stream));
     if (op == OP_LAPLACE)
         e = dispatch_n(c->N, [&](auto nv) { return launch_pcg<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
     else
         e = dispatch_n(c->N, [&](auto nv) { return launch_minres<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
     if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
+    if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    c->stats.kernel_launches++;
+    c->stats.solver_launches++;
     SEM_CUDA(cudaMemcpyAsync(c->h_out, out, sizeof(SolveOut), cudaMemcpyDeviceToHost, c->stream));
     SEM_CUDA(cudaMemcpyAsync(c->h_sync, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, c->stream));
     SEM_CUDA(cudaStreamSynchronize(c->stream));
     if (c->h_sync->err) return fail(SEM_ERR_DEVICE_WAIT, "a grid barrier timed out");
+    if (c->profile) {
+        float ms = 0.f;
+        SEM_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        c->stats.solver_kernel_ms += ms;
+    }
     res->success = c->h_out->success;
     res->n_iter = c->h_out->n_iter;
     res->residual = c->h_out->residual;
     c->stats.krylov_iterations += res->n_iter;
+    c->stats.solver_iterations_fp64 += res->n_iter;
     c->stats.fp64_applies += res->n_iter + 1 + (x_is_zero ? 0 : 1);
     return SEM_OK;
 }
@@ -1105,6 +1128,7 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
                     ze.c[ze.nz++] = ew[l];
                 }
             k_lincomb<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, ze, err);
+            c->stats.kernel_launches++;
             SEM_CUDA(cudaGetLastError());
             double a1 = 0, a2 = 0;
             if ((s = dot_dev(c, err, err, &a1)) || (s = dot_dev(c, err + c->n, err + c->n, &a2))) return s;
@@ -1176,6 +1200,7 @@ extern "C" int sem_schrodinger_bdf2(sem_ctx* c, double* psi_re, double* psi_im, 
             alpha = (2.0 / 3.0) * o->dt;
         } else {
             k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, -1.0 / 3.0, PS[0], 4.0 / 3.0, PS[1], b);
+            c->stats.kernel_launches++;
             SEM_CUDA(cudaGetLastError());
             const double* bb[2] = {b, b + c->n};
             if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res))) return s;

@@ -1,0 +1,57 @@
+"""Small, self-contained workloads for profiling one kernel under ncu.
+
+    python -m schrodingersem_gb300.profile_case --case minres --n 192 --p 8 --maxit 30
+    python -m schrodingersem_gb300.profile_case --case apply --n 192 --p 8 --prec fp32
+
+``minres``: one Schroedinger stage solve (persistent MINRES, capped at
+``maxit`` iterations) on an n x n jittered mesh; ``apply``: a few standalone
+Res applies.  Sizes default to a working set larger than L2 (129 MB) but a
+few hundred MB on the device.
+"""
+from __future__ import annotations
+
+import argparse
+
+import numpy as np
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", default="minres", choices=["minres", "apply"])
+    ap.add_argument("--n", type=int, default=192)
+    ap.add_argument("--p", type=int, default=8)
+    ap.add_argument("--maxit", type=int, default=30)
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--prec", default="fp64", choices=["fp64", "fp32", "mixed"])
+    a = ap.parse_args()
+    import torch
+
+    import schrodingersem_gb300 as S
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.meshgen import gaussian_packet, structured_quads
+    S.build()
+    co, el = structured_quads(a.n, box=(-8.0, 8.0, -8.0, 8.0), jitter=0.1, seed=1)
+    ctx = S.Context(a.p, coords=co, elements=el)
+    X, Y = ctx.node_coords()
+    re, im = gaussian_packet(X, Y, (-2.0, 0.0), 1.0, (3.0, 0.0))
+    V = X * X + Y * Y
+    if a.case == "apply":
+        dt = torch.float64 if a.prec == "fp64" else torch.float32
+        q = [ctx.to_device(t, dt) for t in (re, im, V)]
+        f = ctx.schro_res if a.prec == "fp64" else ctx.schro_res_f32
+        for _ in range(a.reps):
+            f(q[2], 0.01, q[0], q[1])
+        torch.cuda.synchronize()
+        return
+    if a.prec == "mixed":
+        ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    dV = ctx.to_device(V)
+    br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))
+    xr, xi = ctx.zeros(), ctx.zeros()
+    ok, it, res = ctx.minres_schro(dV, 0.0054, xr, xi, br, bi, a.maxit, 1e-10, x_is_zero=True)
+    torch.cuda.synchronize()
+    print(f"minres: success={ok} iterations={it} residual={res:.3e}")
+
+
+if __name__ == "__main__":
+    main()

@@ -109,8 +109,13 @@ def test_schrodinger_drivers(semlib, oracle, known, method, kind):
     assert len(rec) == len(rec_r) == steps
     for (s1, it1), (s2, it2) in zip(rec, rec_r):
         assert s1 == s2 and all(abs(a - b) <= 3 for a, b in zip(it1, it2))
-    err = max(rel_err(gr, pr), rel_err(gi, pi))
-    assert err <= 200 * tol
+    # minres.hpp:92 stops at phibar < tol*|r0| + tol, so with |b| << 1 a stage
+    # is accurate to about tol/|b|: judge both runs against a tight solve
+    tr, ti, _ = om.schrodinger(method, re, im, V, T, dt, 20 * om.dof(), 1e-14)
+    e_gpu = max(rel_err(gr, tr), rel_err(gi, ti))
+    e_ref = max(rel_err(pr, tr), rel_err(pi, ti))
+    assert e_gpu <= 3 * e_ref + 1e-11, (e_gpu, e_ref)
+    assert max(rel_err(gr, pr), rel_err(gi, pi)) <= 4 * e_ref + 1e-11
 
 
 def test_callback_stops_and_state_visible(semlib, oracle, known):
