@@ -231,6 +231,64 @@ def apply_gbs(ctx, torch, reps=20):
     return out
 
 
+FORMS = {
+    # name: (solve precision, inner tolerance, preconditioner, description)
+    "fp64": ("fp64", None, 0, "plain FP64 GPU MINRES (reference algorithm, zero stage guess)"),
+    "mixed": ("mixed", 1e-4, 0, "FP32-inner MINRES in FP64 iterative refinement (true FP64 residual "
+                                "judged by the reference's criterion), zero stage guess"),
+    "mixed_diag": ("mixed", 1e-4, 1, "FP32-inner MINRES with diagonal preconditioner in FP64 iterative "
+                                     "refinement, zero stage guess"),
+}
+
+
+def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
+    """warm-up + timed steps of one solver form, state resident in HBM"""
+    from schrodingersem_gb300 import capi
+    prec, itol, pc, _ = FORMS[form]
+    ctx.set_option(capi.OPT_PRECOND, pc)
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64)
+    if itol:
+        ctx.set_option(capi.OPT_INNER_TOL, itol)
+    dtr = DT / 2.0
+    maxit = 20 * ctx.dof()
+    dre, dim, dV = ctx.to_device(re), ctx.to_device(im), ctx.to_device(Vr)
+    st = torch.cuda.current_stream()
+
+    def one_step(pr, pi, V):
+        if not ctx.schrodinger("dirk4s3", pr, pi, V, 0.5 * dtr, dtr, maxit, TOL):
+            raise RuntimeError(f"{form}: MINRES did not converge")
+
+    for _ in range(warmup):
+        one_step(dre, dim, dV)
+    torch.cuda.synchronize()
+    s0 = ctx.stats()
+    times, iters, sweeps = [], [], []
+    for _ in range(steps):
+        flush_l2(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        one_step(dre, dim, dV)
+        e1.record(st)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1))
+        sts = ctx.stats()
+        iters.append([int(sts.last_stage_iters[k]) for k in range(sts.last_step_stages)])
+        sweeps.append([int(sts.last_stage_sweeps[k]) for k in range(sts.last_step_stages)])
+    s1 = ctx.stats()
+    return {
+        "ms": float(np.mean(times)), "state": (dre.cpu().numpy(), dim.cpu().numpy()),
+        "iters_per_step": float(np.mean([np.sum(i) for i in iters])),
+        "iters_per_stage": float(np.mean([np.mean(i) for i in iters])),
+        "sweeps_per_stage": float(np.mean([np.mean(i) for i in sweeps])),
+        "launches": int(s1.kernel_launches - s0.kernel_launches),
+        "solver_ms": s1.solver_kernel_ms - s0.solver_kernel_ms,
+        "it64": s1.solver_iterations_fp64 - s0.solver_iterations_fp64,
+        "it32": s1.solver_iterations_fp32 - s0.solver_iterations_fp32,
+        "applies64": s1.fp64_applies - s0.fp64_applies,
+        "one_step": one_step,
+    }
+
+
 def run_ours(args):
     import torch
 
@@ -264,104 +322,96 @@ def run_ours(args):
     nrm = mass_norm(J, w, re, im)
     re, im = re / nrm, -im / nrm                     # psi' = conj(psi)
     Vr = X * X + Y * Y                               # V' = 2 * (x^2+y^2)/2
-    dtr = DT / 2.0
-    maxit = 20 * ctx.dof()
-    dre, dim = ctx.to_device(re), ctx.to_device(im)
-    dV = ctx.to_device(Vr)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    st = torch.cuda.current_stream()
-
-    def one_step(pr, pi, V):
-        ok = ctx.schrodinger("dirk4s3", pr, pi, V, 0.5 * dtr, dtr, maxit, TOL)
-        if not ok:
-            raise RuntimeError("MINRES did not converge")
-
-    # warm-up
-    for _ in range(args.warmup):
-        one_step(dre, dim, dV)
-    torch.cuda.synchronize()
-    s0 = ctx.stats()
-    iters = []
-    times = []
+    forms = [f for f in args.forms.split(",") if f]
+    res = {}
     with ClockSampler(local) as clk:
         if dist:
             dist.barrier()
-        torch.cuda.synchronize()
-        for _ in range(args.steps):
-            flush_l2(flush)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(st)
-            one_step(dre, dim, dV)
-            e1.record(st)
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1))
-            sts = ctx.stats()
-            iters.append([int(sts.last_stage_iters[k]) for k in range(sts.last_step_stages)])
-        torch.cuda.synchronize()
+        for f in forms:
+            res[f] = run_form(ctx, torch, f, re, im, Vr, args.steps, args.warmup, flush)
         if dist:
             dist.barrier()
-    s1 = ctx.stats()
-    ms = float(np.sum(times)) / args.steps
+    # accuracy of every form against the plain FP64 solve (M-weighted L2)
+    ref_state = res["fp64"]["state"] if "fp64" in res else None
+    for f, r in res.items():
+        if ref_state is None:
+            r["rel_err_vs_fp64"] = None
+            continue
+        dr, di = r["state"][0] - ref_state[0], r["state"][1] - ref_state[1]
+        r["rel_err_vs_fp64"] = mass_norm(J, w, dr, di) / mass_norm(J, w, *ref_state)
+    valid = [f for f in forms if res[f]["rel_err_vs_fp64"] is None or res[f]["rel_err_vs_fp64"] <= 1e-8]
+    head = min(valid, key=lambda f: res[f]["ms"])
+    H = res[head]
+    ms = H["ms"]
     if dist:
         t = torch.tensor([ms], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
-    launches = int(s1.kernel_launches - s0.kernel_launches)
-    sol_ms = s1.solver_kernel_ms - s0.solver_kernel_ms
-    sol_it = s1.solver_iterations_fp64 - s0.solver_iterations_fp64
-    sol_launch = s1.solver_launches - s0.solver_launches
 
-    # e2e through the C ABI with pinned host buffers
+    # e2e of the headline form through the C ABI with pinned host buffers
     h_re = torch.from_numpy(re.copy()).pin_memory()
     h_im = torch.from_numpy(im.copy()).pin_memory()
     h_V = torch.from_numpy(np.ascontiguousarray(Vr)).pin_memory()
+    prec = FORMS[head][0]
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64)
+    st = torch.cuda.current_stream()
     for _ in range(min(2, args.warmup)):
-        one_step(h_re.numpy(), h_im.numpy(), h_V.numpy())
+        H["one_step"](h_re.numpy(), h_im.numpy(), h_V.numpy())
     e2e_times = []
     for _ in range(args.steps):
         flush_l2(flush)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st)
-        one_step(h_re.numpy(), h_im.numpy(), h_V.numpy())
+        H["one_step"](h_re.numpy(), h_im.numpy(), h_V.numpy())
         e1.record(st)
         torch.cuda.synchronize()
         e2e_times.append(e0.elapsed_time(e1))
     e2e_s = float(np.mean(e2e_times)) / 1e3
     nbytes = ctx.n * 8
-
     if rank != 0:
         return
     app = apply_gbs(ctx, torch)
-    # MINRES iteration: one Res apply (9 words/node) + 13 two-plane vector words
-    bytes_per_iter = ctx.n * 8 * (9 + 26)
-    achieved = bytes_per_iter * sol_it / (sol_ms / 1e3) / 1e9 if sol_ms > 0 else None
-    flops_per_iter = ctx.n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
-    iters_per_step = float(np.mean([np.sum(i) for i in iters]))
-    cpu = cpu_baseline_sample(iters_per_step) if not args.no_cpu else None
+    # algorithmic bytes of the dominant kernel (the persistent solver):
+    # per Krylov iteration one Res apply (9 words/node) + 13 two-plane vector
+    # words; per FP64 refinement sweep one FP64 residual (apply + 5 words)
+    n = ctx.n
+    b64, b32 = n * 8 * (9 + 26), n * 4 * (9 + 26)
+    sweeps_total = H["applies64"] if prec == "mixed" else 0
+    alg_bytes = H["it64"] * b64 + H["it32"] * b32 + sweeps_total * n * 8 * 14
+    achieved = alg_bytes / (H["solver_ms"] / 1e3) / 1e9 if H["solver_ms"] > 0 else None
+    kern = "k_minres_mixed<9,RES>" if prec == "mixed" else "k_minres<9,double,RES>"
+    forms_out = {f: {"s_per_step": r["ms"] / 1e3, "minres_iters_per_stage": r["iters_per_stage"],
+                     "refine_sweeps_per_stage": r["sweeps_per_stage"], "rel_err_vs_fp64": r["rel_err_vs_fp64"],
+                     "description": FORMS[f][3]} for f, r in res.items()}
+    cpu = cpu_baseline_sample(res["fp64"]["iters_per_step"] if "fp64" in res else H["iters_per_step"]) \
+        if not args.no_cpu else None
+    flops64 = n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
     line = {
         "metric": METRIC, "value": ms / 1e3, "unit": "s/step", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": "plain FP64 GPU MINRES (reference algorithm, zero stage guess)",
+        "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f64+f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": FORMS[head][3],
                    "l2": "flushed before every step (256 MiB write)", "parallelism": "replicas only"},
+        "forms": forms_out,
+        "speedup_vs_plain_fp64": (res["fp64"]["ms"] / ms) if "fp64" in res else None,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
-                     "kernel": "k_minres<9,double,RES> (persistent cooperative MINRES)",
-                     "bytes_per_iteration": bytes_per_iter, "iterations": sol_it,
-                     "launches": sol_launch, "kernel_ms": sol_ms, "peak_source": peak_src,
-                     "fp64_pipe": {"achieved_tflops": flops_per_iter * sol_it / (sol_ms / 1e3) / 1e12
-                                   if sol_ms > 0 else None, "peak_tflops": 1.19,
-                                   "peak_source": "FMA-chain probe on this pool's GB300"}},
+                     "kernel": kern + " (persistent cooperative solver)",
+                     "algorithmic_bytes": alg_bytes, "fp64_iterations": H["it64"], "fp32_iterations": H["it32"],
+                     "kernel_ms": H["solver_ms"], "peak_source": peak_src,
+                     "fp64_pipe": ({"achieved_tflops": flops64 * H["it64"] / (H["solver_ms"] / 1e3) / 1e12,
+                                    "peak_tflops": 1.19, "peak_source": "FMA-chain probe on this pool's GB300"}
+                                   if prec == "fp64" and H["solver_ms"] > 0 else None)},
         "apply": {"fp64_gbs": app["fp64"]["gbs"], "fp32_gbs": app["fp32"]["gbs"],
                   "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak, "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
                   "bytes_fp64": app["fp64"]["bytes"], "note": "n_loc*s*9 words, L2 flushed before each apply"},
-        "minres_iters_per_stage": float(np.mean([np.mean(i) for i in iters])),
         "cpu_baseline": cpu,
         "e2e": {"value": e2e_s, "unit": "s/step", "h2d_bytes_per_step": 3 * nbytes,
                 "d2h_bytes_per_step": 2 * nbytes},
         "clocks": clk.summary(),
-        "gpu_launches": launches,
+        "gpu_launches": H["launches"],
     }
     print(json.dumps(line), flush=True)
     if dist:
@@ -375,6 +425,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--forms", default="fp64,mixed,mixed_diag", help="solver forms to time (comma list)")
     args = ap.parse_args()
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:

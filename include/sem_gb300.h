@@ -61,9 +61,14 @@ enum sem_option {
     SEM_OPT_STAGE_GUESS = 3,     /* SEM_GUESS_ZERO (reference), _EXTRAPOLATE, _LEARNED */
     SEM_OPT_WAIT_TIMEOUT_MS = 4, /* limit of every device-side wait (default 2000 ms) */
     SEM_OPT_MAX_REFINE = 5,      /* cap on FP64 refinement sweeps in mixed mode (default 50) */
-    SEM_OPT_PROFILE = 6          /* 1: time every persistent solver launch with CUDA events */
+    SEM_OPT_PROFILE = 6,         /* 1: time every persistent solver launch with CUDA events */
+    SEM_OPT_PRECOND = 7          /* preconditioner of the FP32 inner solve in mixed mode:
+                                    SEM_PRECOND_NONE (default, as the reference) or
+                                    SEM_PRECOND_DIAG (diagonal of |A|); the FP64 outer test
+                                    on the true residual is unchanged */
 };
 enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
+enum { SEM_PRECOND_NONE = 0, SEM_PRECOND_DIAG = 1 };
 enum { SEM_GUESS_ZERO = 0, SEM_GUESS_EXTRAPOLATE = 1, SEM_GUESS_LEARNED = 2 };
 
 typedef struct sem_ctx sem_ctx;

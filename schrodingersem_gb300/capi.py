@@ -85,7 +85,9 @@ SIGNATURES = {
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
+OPT_PRECOND = 7
 PREC_FP64, PREC_MIXED = 0, 1
+PRECOND_NONE, PRECOND_DIAG = 0, 1
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 
 _lib = None

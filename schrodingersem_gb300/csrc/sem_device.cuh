@@ -24,6 +24,12 @@ __host__ __device__ constexpr int geo_tpb(int N)
     return ((geo_k(N) * N * N + 31) / 32) * 32;
 }
 
+// blocks per SM the persistent kernels are compiled for (caps registers at 128)
+__host__ __device__ constexpr int geo_minb(int N)
+{
+    return geo_tpb(N) <= 256 ? 2 : 1;
+}
+
 template <int OP>
 __host__ __device__ constexpr int op_nc()
 {
@@ -235,6 +241,133 @@ __device__ __forceinline__ void apply_chunk(ApplySmem<N, T, OP>& s, const Fac<T>
 #pragma unroll
             for (int k = 0; k < N; ++k) a = fma(s.D[k * N + j], f2[i + k * N], a);
             lap[c] = a;
+        }
+        T o[NC];
+        if (OP == OP_LAPLACE) {
+            o[0] = lap[0];
+        } else if (OP == OP_HELM) {
+            o[0] = lap[0] + (ms * pv) * u[0];
+        } else if (OP == OP_RES) {
+            const T mv = ms * pv;
+            const T Lv = lap[NC - 1] + mv * u[NC - 1];
+            const T Lu = lap[0] + mv * u[0];
+            o[0] = ms * u[0] + alpha * Lv;
+            o[NC - 1] = alpha * Lu - ms * u[NC - 1];
+        } else {  // OP_F
+            const T mv = ms * pv;
+            o[0] = -(lap[NC - 1] + mv * u[NC - 1]);
+            o[NC - 1] = -(lap[0] + mv * u[0]);
+        }
+        store(e, i, j, flat, o);
+    }
+    __syncthreads();
+}
+
+// ----------------------------------------------- range-staged element apply
+// The persistent solvers give every block a contiguous element range and
+// stage up to kmax elements of it in dynamic shared memory at once, every
+// thread looping over several nodes in each sub-phase.  All loads of the
+// staged range are issued before the first barrier, so one pass costs one
+// memory latency instead of one per small chunk.
+// Shared layout (type T): D[NN] | u[NC][kmax*NN] | f1[NC][kmax*NN] | f2[NC][kmax*NN]
+template <int N, typename T, int OP>
+__host__ __device__ constexpr size_t range_smem_bytes(int kmax)
+{
+    return sizeof(T) * ((size_t)N * N + 3ull * op_nc<OP>() * (size_t)kmax * N * N);
+}
+
+template <int N, typename T>
+__device__ __forceinline__ void load_dmat_raw(T* sm, const DevMesh& m)
+{
+    const T* D = dmat_of<T>(m);
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) sm[t] = D[t];
+}
+
+// One block-wide pass over elements [e0, e0+ne), ne <= kmax.  Every thread
+// of the block must call it.  Same operator and callbacks as apply_chunk.
+template <int N, typename T, int OP, class Load, class Store>
+__device__ __forceinline__ void apply_range(T* sm, int kmax, const Fac<T>& fac,
+                                            const T* __restrict__ pot, T alpha, int e0, int ne,
+                                            Load&& load, Store&& store)
+{
+    constexpr int NN = N * N;
+    constexpr int NC = op_nc<OP>();
+    const int total = ne * NN;
+    const int st = kmax * NN;
+    const T* D = sm;
+    T* su = sm + NN;
+    T* sf1 = su + NC * st;
+    T* sf2 = sf1 + NC * st;
+    // 1. inputs of the whole range
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int e = e0 + le;
+        T u[NC];
+        load(e, node % N, node / N, (long long)e * NN + node, u);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) su[c * st + t] = u[c];
+    }
+    __syncthreads();
+    if (OP == OP_MASS) {
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int le = t / NN;
+            const int node = t - le * NN;
+            const int e = e0 + le;
+            const long long flat = (long long)e * NN + node;
+            T o[NC];
+            o[0] = __ldg(fac.mass + flat) * su[t];
+            store(e, node % N, node / N, flat, o);
+        }
+        __syncthreads();
+        return;
+    }
+    // 2. contravariant fluxes
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int i = node % N, j = node / N;
+        const long long flat = (long long)(e0 + le) * NN + node;
+        const T g11 = __ldg(fac.g11 + flat), g12 = __ldg(fac.g12 + flat), g22 = __ldg(fac.g22 + flat);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* uc = su + c * st + le * NN;
+            T ur = T(0), us = T(0);
+#pragma unroll
+            for (int k = 0; k < N; ++k) {
+                ur = fma(D[i * N + k], uc[k + j * N], ur);  // (D u)(i,j)
+                us = fma(D[j * N + k], uc[i + k * N], us);  // (u D^T)(i,j)
+            }
+            sf1[c * st + t] = g11 * ur - g12 * us;
+            sf2[c * st + t] = g22 * us - g12 * ur;
+        }
+    }
+    __syncthreads();
+    // 3. weak divergence + mass/potential terms
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int i = node % N, j = node / N;
+        const int e = e0 + le;
+        const long long flat = (long long)e * NN + node;
+        T ms = T(0), pv = T(0);
+        if (OP != OP_LAPLACE) ms = __ldg(fac.mass + flat);
+        if (OP == OP_HELM || OP == OP_RES || OP == OP_F) pv = __ldg(pot + flat);
+        T lap[NC], u[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* f1 = sf1 + c * st + le * NN;
+            const T* f2 = sf2 + c * st + le * NN;
+            T a = T(0);
+#pragma unroll
+            for (int k = 0; k < N; ++k) a = fma(D[k * N + i], f1[k + j * N], a);
+#pragma unroll
+            for (int k = 0; k < N; ++k) a = fma(D[k * N + j], f2[i + k * N], a);
+            lap[c] = a;
+            u[c] = su[c * st + t];
         }
         T o[NC];
         if (OP == OP_LAPLACE) {

@@ -76,6 +76,31 @@ __global__ void k_to_f32(long long n, const double* __restrict__ a, float* __res
 
 static int grid_1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 16); }
 
+// dynamic shared memory a persistent solver block may use for staging
+static const size_t kSolverSmemBudget = 160 * 1024;
+
+// Diagonal preconditioner P^-1 (continuous format).  Res = [M, aL; aL, -M]:
+// P = diag(d, d), d = sqrt(m^2 + a^2 (k + m V)^2), the diagonal of |Res|
+// when M and L are replaced by their diagonals.  Helmholtz K + M c:
+// d = k + m |c|.  m, k: assembled mass and stiffness diagonals.
+__global__ void k_prec(long long n, int op, double alpha, const double* __restrict__ mdiag,
+                       const double* __restrict__ kdiag, const double* __restrict__ pot,
+                       float* __restrict__ pinv)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double m = mdiag[i], k = kdiag[i];
+        double d;
+        if (op == OP_RES) {
+            const double l = k + m * pot[i];
+            d = sqrt(m * m + alpha * alpha * l * l);
+        } else {
+            d = k + m * fabs(pot[i]);
+        }
+        pinv[i] = (float)(1.0 / d);
+    }
+}
+
 // --------------------------------------------------------------- quadrature
 static double legendre(int n, double x)
 {
@@ -190,6 +215,7 @@ struct sem_ctx {
     double timeout_ms = 2000.0;
     int max_refine = 50;
     bool profile = false;
+    int precond = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     sem_stats stats{};
     // workspace
@@ -409,6 +435,45 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
                 ms[k] = ww * Jv;
             }
     }
+    // diagonals of the assembled stiffness and lumped mass (continuous format),
+    // for the diagonal preconditioner.  Element-local diagonal of the weak
+    // Laplacian: sum_k D(k,i)^2 g11(k,j) + sum_k D(k,j)^2 g22(i,k) - 2 D(i,i) D(j,j) g12(i,j)
+    std::vector<double> kloc(c->n), kdiag(c->n), mdiag(c->n);
+    for (int e = 0; e < n_el; ++e)
+        for (int j = 0; j < N; ++j)
+            for (int i = 0; i < N; ++i) {
+                const size_t b = (size_t)e * NN;
+                double s = 0.0;
+                for (int k = 0; k < N; ++k) {
+                    const double dki = c->D[k + i * N], dkj = c->D[k + j * N];
+                    s += dki * dki * g11[b + k + (size_t)j * N] + dkj * dkj * g22[b + i + (size_t)k * N];
+                }
+                s -= 2.0 * c->D[i + i * N] * c->D[j + j * N] * g12[b + i + (size_t)j * N];
+                kloc[b + i + (size_t)j * N] = s;
+            }
+    auto assemble = [&](const std::vector<double>& loc, std::vector<double>& out) {
+        for (int e = 0; e < n_el; ++e)
+            for (int j = 0; j < N; ++j)
+                for (int i = 0; i < N; ++i) {
+                    const size_t f = (size_t)e * NN + i + (size_t)j * N;
+                    const bool ib = (i == 0 || i == N - 1), jb = (j == 0 || j == N - 1);
+                    double v = loc[f];
+                    if (ib && jb) {
+                        const int cc = (j == 0) ? (i == 0 ? 0 : 1) : (i == 0 ? 3 : 2);
+                        const int node = cnode[4 * e + cc];
+                        v = 0.0;
+                        for (int q = nptr[node]; q < nptr[node + 1]; ++q) v += loc[nflat[q]];
+                    } else if (ib || jb) {
+                        const int sd = jb ? (j == 0 ? 0 : 2) : (i == N - 1 ? 1 : 3);
+                        const int k = jb ? i : j;
+                        if (!(fl[e] & (16 << sd))) v += loc[(size_t)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd])];
+                    }
+                    out[f] = v;
+                }
+    };
+    assemble(kloc, kdiag);
+    assemble(ms, mdiag);
+
     // device copies
     DevMesh& d = c->dm;
     d.N = N;
@@ -435,7 +500,8 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, Drowf, &d.D32)) || (s = upload(c, g11, &d.g11)) || (s = upload(c, g12, &d.g12)) ||
         (s = upload(c, g22, &d.g22)) || (s = upload(c, ms, &d.mass)) ||
         (s = upload(c, tof(g11), &d.g11f)) || (s = upload(c, tof(g12), &d.g12f)) ||
-        (s = upload(c, tof(g22), &d.g22f)) || (s = upload(c, tof(ms), &d.massf)))
+        (s = upload(c, tof(g22), &d.g22f)) || (s = upload(c, tof(ms), &d.massf)) ||
+        (s = upload(c, kdiag, &d.kdiag)) || (s = upload(c, mdiag, &d.mdiag)))
         return s;
     SEM_CUDA(cudaMallocHost((void**)&c->h_out, sizeof(SolveOut)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_sync, sizeof(GridSync)));
@@ -572,6 +638,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_MAX_REFINE:
             if (!(v >= 1)) return fail(SEM_ERR_ARG, "max refine must be >= 1");
             c->max_refine = (int)v;
+            return SEM_OK;
+        case SEM_OPT_PRECOND:
+            if (v != SEM_PRECOND_NONE && v != SEM_PRECOND_DIAG) return fail(SEM_ERR_ARG, "bad preconditioner");
+            c->precond = (int)v;
             return SEM_OK;
         case SEM_OPT_PROFILE:
             c->profile = v != 0;
@@ -813,26 +883,80 @@ static int krylov_work(sem_ctx* c, int nc, KrylovWork<double>* w, GridSync** syn
     return SEM_OK;
 }
 
-static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
-                      const double* const b[2], int maxit, double tol, int x_is_zero,
-                      sem_solver_results* res)
+static int finish_solve(sem_ctx* c, SolveOut* out, GridSync* sync, sem_solver_results* res)
+{
+    SEM_CUDA(cudaMemcpyAsync(c->h_out, out, sizeof(SolveOut), cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(c->h_sync, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->h_sync->err) return fail(SEM_ERR_DEVICE_WAIT, "a grid barrier timed out");
+    if (c->profile) {
+        float ms = 0.f;
+        SEM_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+        c->stats.solver_kernel_ms += ms;
+    }
+    res->success = c->h_out->success;
+    res->n_iter = c->h_out->n_iter;
+    res->residual = c->h_out->residual;
+    c->stats.krylov_iterations += res->n_iter;
+    return SEM_OK;
+}
+
+// FP64 refinement around an FP32 inner MINRES (SEM_PREC_MIXED)
+static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
+                     const double* const b[2], int maxit, double tol, int x_is_zero,
+                     sem_solver_results* res, int* sweeps)
 {
     const int nc = (op == OP_RES) ? 2 : 1;
-    KrylovWork<double> w{};
+    const size_t v = (size_t)nc * c->n;
+    KrylovWork<float> w{};
+    const char* ln[3] = {"k32_L0", "k32_L1", "k32_L2"};
+    const char* wn[3] = {"k32_W0", "k32_W1", "k32_W2"};
+    const char* yn[2] = {"k32_Y0", "k32_Y1"};
+    int s = 0;
+    for (int k = 0; k < 3; ++k)
+        if ((s = wsget(c, ln[k], v, &w.L[k])) || (s = wsget(c, wn[k], v, &w.W[k]))) return s;
+    for (int k = 0; k < 2; ++k)
+        if ((s = wsget(c, yn[k], v, &w.Y[k]))) return s;
     GridSync* sync = nullptr;
     SolveOut* out = nullptr;
-    int s = krylov_work(c, nc, &w, &sync, &out);
-    if (s) return s;
-    int grid = 0;
+    double *r64 = nullptr, *Y64 = nullptr;
+    float *x32 = nullptr, *pot32 = nullptr;
+    if ((s = wsget(c, "kr_part", 2 * 152 * 64, &w.partials)) || (s = wsget(c, "kr_sync", 1, &sync)) ||
+        (s = wsget(c, "kr_out", 1, &out)) || (s = wsget(c, "mx_r64", v, &r64)) ||
+        (s = wsget(c, "mx_Y64", v, &Y64)) || (s = wsget(c, "mx_x32", v, &x32)) ||
+        (s = wsget(c, "mx_pot32", c->n, &pot32)))
+        return s;
+    k_to_f32<<<grid_1d(c->n), 256, 0, c->stream>>>(c->n, pot, pot32);
+    c->stats.kernel_launches++;
+    SEM_CUDA(cudaGetLastError());
+    MixedArgs mx{};
+    mx.inner_tol = c->inner_tol;
+    mx.max_sweeps = c->max_refine;
+    mx.inner_maxit = maxit;
+    for (int q = 0; q < 2; ++q) {
+        mx.r64[q] = r64 + (size_t)q * c->n;
+        mx.Y64[q] = Y64 + (size_t)q * c->n;
+        mx.x32[q] = x32 + (size_t)q * c->n;
+    }
+    mx.pot32 = pot32;
+    mx.pinv32 = nullptr;
+    if (c->precond) {
+        float* pinv = nullptr;
+        if ((s = wsget(c, "mx_pinv32", c->n, &pinv))) return s;
+        k_prec<<<grid_1d(c->n), 256, 0, c->stream>>>(c->n, op, alpha, c->dm.mdiag, c->dm.kdiag, pot, pinv);
+        c->stats.kernel_launches++;
+        SEM_CUDA(cudaGetLastError());
+        mx.pinv32 = pinv;
+    }
+    int grid = 0, kmax = 1;
+    size_t smem = 0;
     dispatch_n(c->N, [&](auto nv) {
-        grid = solver_grid<decltype(nv)::value>(op, nc, c->sms);
+        grid = solver_plan<decltype(nv)::value>(op, true, c->E, c->sms, kSolverSmemBudget, &kmax, &smem);
         return cudaSuccess;
     });
     if (grid <= 0) return fail(SEM_ERR_CUDA, "could not size the cooperative grid");
-    const int chunks = (c->E + 0) / 1;  // one block needs at least one element
-    grid = std::min(grid, std::max(1, chunks));
-    grid = std::min(grid, 152 * 64);
     SolveArgs a{};
+    a.kmax = kmax;
     a.op = op;
     a.nc = nc;
     a.pot = pot;
@@ -849,29 +973,73 @@ static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, doubl
     a.out = out;
     SEM_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), c->stream));
     SEM_CUDA(cudaMemsetAsync(out, 0, sizeof(SolveOut), c->stream));
-    cudaError_t e;
     if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[0], c->stream));
-    if (op == OP_LAPLACE)
-        e = dispatch_n(c->N, [&](auto nv) { return launch_pcg<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
-    else
-        e = dispatch_n(c->N, [&](auto nv) { return launch_minres<decltype(nv)::value>(c->dm, a, w, grid, c->stream); });
+    cudaError_t e = dispatch_n(c->N, [&](auto nv) {
+        return launch_solver<decltype(nv)::value>(c->dm, a, &w, &mx, grid, smem, c->stream);
+    });
     if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
     if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[1], c->stream));
     c->stats.kernel_launches++;
     c->stats.solver_launches++;
-    SEM_CUDA(cudaMemcpyAsync(c->h_out, out, sizeof(SolveOut), cudaMemcpyDeviceToHost, c->stream));
-    SEM_CUDA(cudaMemcpyAsync(c->h_sync, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, c->stream));
-    SEM_CUDA(cudaStreamSynchronize(c->stream));
-    if (c->h_sync->err) return fail(SEM_ERR_DEVICE_WAIT, "a grid barrier timed out");
-    if (c->profile) {
-        float ms = 0.f;
-        SEM_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
-        c->stats.solver_kernel_ms += ms;
+    if ((s = finish_solve(c, out, sync, res))) return s;
+    *sweeps = c->h_out->sweeps;
+    c->stats.solver_iterations_fp32 += res->n_iter;
+    c->stats.fp32_applies += res->n_iter + *sweeps;
+    c->stats.fp64_applies += *sweeps + 1;
+    return SEM_OK;
+}
+
+static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
+                      const double* const b[2], int maxit, double tol, int x_is_zero,
+                      sem_solver_results* res, int* sweeps = nullptr)
+{
+    if (sweeps) *sweeps = 1;
+    if (c->prec == SEM_PREC_MIXED && op != OP_LAPLACE) {
+        int sw = 0;
+        int s = run_mixed(c, op, pot, alpha, x, b, maxit, tol, x_is_zero, res, &sw);
+        if (sweeps) *sweeps = sw;
+        return s;
     }
-    res->success = c->h_out->success;
-    res->n_iter = c->h_out->n_iter;
-    res->residual = c->h_out->residual;
-    c->stats.krylov_iterations += res->n_iter;
+    const int nc = (op == OP_RES) ? 2 : 1;
+    KrylovWork<double> w{};
+    GridSync* sync = nullptr;
+    SolveOut* out = nullptr;
+    int s = krylov_work(c, nc, &w, &sync, &out);
+    if (s) return s;
+    int grid = 0, kmax = 1;
+    size_t smem = 0;
+    dispatch_n(c->N, [&](auto nv) {
+        grid = solver_plan<decltype(nv)::value>(op, false, c->E, c->sms, kSolverSmemBudget, &kmax, &smem);
+        return cudaSuccess;
+    });
+    if (grid <= 0) return fail(SEM_ERR_CUDA, "could not size the cooperative grid");
+    SolveArgs a{};
+    a.kmax = kmax;
+    a.op = op;
+    a.nc = nc;
+    a.pot = pot;
+    a.alpha = alpha;
+    a.b[0] = b[0];
+    a.b[1] = nc == 2 ? b[1] : nullptr;
+    a.x[0] = x[0];
+    a.x[1] = nc == 2 ? x[1] : nullptr;
+    a.maxit = maxit;
+    a.tol = tol;
+    a.x_is_zero = x_is_zero;
+    a.timeout_ns = (long long)(c->timeout_ms * 1e6);
+    a.sync = sync;
+    a.out = out;
+    SEM_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), c->stream));
+    SEM_CUDA(cudaMemsetAsync(out, 0, sizeof(SolveOut), c->stream));
+    if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[0], c->stream));
+    cudaError_t e = dispatch_n(c->N, [&](auto nv) {
+        return launch_solver<decltype(nv)::value>(c->dm, a, &w, nullptr, grid, smem, c->stream);
+    });
+    if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
+    if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[1], c->stream));
+    c->stats.kernel_launches++;
+    c->stats.solver_launches++;
+    if ((s = finish_solve(c, out, sync, res))) return s;
     c->stats.solver_iterations_fp64 += res->n_iter;
     c->stats.fp64_applies += res->n_iter + 1 + (x_is_zero ? 0 : 1);
     return SEM_OK;
@@ -1034,12 +1202,12 @@ static int schro_rhs(SchroRun* r, double dt, const ZList& zl, double* b)
 }
 
 static int schro_stage_solve(SchroRun* r, double alpha, const double* b, double* z, int max_iter,
-                             double tol, int x_is_zero, sem_solver_results* res)
+                             double tol, int x_is_zero, sem_solver_results* res, int* sweeps)
 {
     sem_ctx* c = r->c;
     double* x[2] = {z, z + c->n};
     const double* bb[2] = {b, b + c->n};
-    return run_krylov(c, OP_RES, r->V, alpha, x, bb, max_iter, tol, x_is_zero, res);
+    return run_krylov(c, OP_RES, r->V, alpha, x, bb, max_iter, tol, x_is_zero, res, sweeps);
 }
 
 static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, const double* V,
@@ -1098,9 +1266,10 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             double* z = Z + (size_t)st * 2 * c->n;
             SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
             sem_solver_results res{};
-            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, 1, &res))) return s;
+            int sw = 1;
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, 1, &res, &sw))) return s;
             c->stats.last_stage_iters[st] = res.n_iter;
-            c->stats.last_stage_sweeps[st] = 1;
+            c->stats.last_stage_sweeps[st] = sw;
             if (!res.success) {
                 ok = false;
                 break;
@@ -1192,21 +1361,22 @@ extern "C" int sem_schrodinger_bdf2(sem_ctx* c, double* psi_re, double* psi_im, 
         if ((s = apply_galerkin(c, OP_MASS, nullptr, 0.0, p + c->n, nullptr, dst + c->n, nullptr, -1.0))) return s;
         ++nps;
         sem_solver_results res{};
+        int sw = 1;
         double* x[2] = {p, p + c->n};
         c->stats.last_step_stages = 1;
         if (nps == 1) {
             const double* bb[2] = {PS[0], PS[0] + c->n};
-            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res))) return s;
+            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res, &sw))) return s;
             alpha = (2.0 / 3.0) * o->dt;
         } else {
             k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, -1.0 / 3.0, PS[0], 4.0 / 3.0, PS[1], b);
             c->stats.kernel_launches++;
             SEM_CUDA(cudaGetLastError());
             const double* bb[2] = {b, b + c->n};
-            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res))) return s;
+            if ((s = run_krylov(c, OP_RES, r.V, alpha, x, bb, o->max_iter, o->tol, 0, &res, &sw))) return s;
         }
         c->stats.last_stage_iters[0] = res.n_iter;
-        c->stats.last_stage_sweeps[0] = 1;
+        c->stats.last_stage_sweeps[0] = sw;
         if ((s = sem_unmask(c, p)) || (s = sem_unmask(c, p + c->n))) return s;
         t += o->dt;
         if (!res.success) {

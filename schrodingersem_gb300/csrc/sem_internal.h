@@ -45,6 +45,8 @@ struct DevMesh {
     const int* corner_node = nullptr;// [E*4] corner node id
     const int* node_ptr = nullptr;   // [n_nodes+1] CSR over copies of each corner node
     const int* node_flat = nullptr;  // flat indices of the copies, element order
+    const double* kdiag = nullptr;   // diagonal of the assembled stiffness (continuous format)
+    const double* mdiag = nullptr;   // assembled lumped mass w_i w_j J (continuous format)
     const double* D64 = nullptr;     // D row-major: D(i,k) at [i*N+k]
     const float* D32 = nullptr;
     // premultiplied factors w_i w_j {A, B, C, J}
@@ -89,9 +91,23 @@ struct SolveArgs {
     int maxit;
     double tol;
     int x_is_zero;
+    int kmax;         // elements staged per pass (solver_plan)
     long long timeout_ns;
     GridSync* sync;
     SolveOut* out;
+};
+
+// Mixed-precision refinement: FP64 true residual and solution, FP32 inner
+// MINRES (see k_minres_mixed).
+struct MixedArgs {
+    double inner_tol;
+    int max_sweeps;
+    int inner_maxit;
+    double* r64[2];      // FP64 residual planes
+    double* Y64[2];      // FP64 element-local output planes
+    float* x32[2];       // FP32 correction planes
+    const float* pot32;  // FP32 copy of the potential (V or c)
+    const float* pinv32; // diagonal preconditioner P^-1 (continuous format), or null
 };
 
 // ---- launchers, one explicit instantiation per N in sem_inst.cu -------------
@@ -124,16 +140,16 @@ cudaError_t launch_combo_f(const DevMesh& m, const double* V, const double* p, c
 template <int N>
 cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl, double* p_out,
                           cudaStream_t st);
-// persistent Krylov solvers (cooperative launch)
+// persistent Krylov solvers (cooperative launch).  solver_plan picks the grid
+// (at most one block per SM) and the per-pass staging capacity in elements;
+// launch_solver runs MINRES (op OP_RES/OP_HELM), PCG (OP_LAPLACE) or, when
+// mx is given, the mixed-precision refinement.  work points to a
+// KrylovWork<double> (FP64 solvers) or KrylovWork<float> (mixed).
 template <int N>
-cudaError_t launch_minres(const DevMesh& m, const SolveArgs& a, const KrylovWork<double>& w,
-                          int grid, cudaStream_t st);
+int solver_plan(int op, bool mixed, int E, int sms, size_t smem_budget, int* kmax, size_t* smem);
 template <int N>
-cudaError_t launch_pcg(const DevMesh& m, const SolveArgs& a, const KrylovWork<double>& w,
-                       int grid, cudaStream_t st);
-// co-resident grid size for the persistent solvers
-template <int N>
-int solver_grid(int op, int nc, int sms);
+cudaError_t launch_solver(const DevMesh& m, const SolveArgs& a, const void* work, const MixedArgs* mx,
+                          int grid, size_t smem, cudaStream_t st);
 
 }  // namespace semgb
 

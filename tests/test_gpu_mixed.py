@@ -1,0 +1,110 @@
+"""FP32-inner MINRES inside FP64 iterative refinement.
+
+The refinement stops on the true FP64 residual with the reference's own
+criterion (|r| < tol |r_0| + tol, minres.hpp:92), so its solutions must agree
+with the plain FP64 solver's to the accuracy the metric asks for (1e-8
+relative L2) and meet the residual criterion themselves."""
+import numpy as np
+import pytest
+
+from tests.util import SMALL_MESH, rel_err, structured
+
+pytestmark = pytest.mark.gpu
+
+
+def _packet_case(semlib, oracle, n=8, p=6):
+    co, el = structured(n, box=(-4, 4, -4, 4), jitter=0.1, seed=2)
+    ctx = semlib.Context(p, coords=co, elements=el)
+    om = oracle.Mesh(p, coords=co, elements=el)
+    from schrodingersem_gb300.meshgen import gaussian_packet
+    X, Y = om.node_coords()
+    re, im = gaussian_packet(X, Y, (-1.0, 0.5), 0.8, (3.0, -1.0))
+    return ctx, om, re, im, X * X + Y * Y
+
+
+def test_mixed_stage_solve_meets_fp64_criterion(semlib, oracle):
+    from schrodingersem_gb300 import capi
+    ctx, om, re, im, V = _packet_case(semlib, oracle)
+    dV = ctx.to_device(V)
+    br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))
+    br.mul_(0.005)
+    bi.mul_(0.005)
+    alpha, tol = 0.005 * 1.0886, 1e-10
+    xr, xi = ctx.zeros(), ctx.zeros()
+    ok64, it64, _ = ctx.minres_schro(dV, alpha, xr, xi, br, bi, 20 * ctx.dof(), tol, x_is_zero=True)
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    yr, yi = ctx.zeros(), ctx.zeros()
+    okm, itm, resm = ctx.minres_schro(dV, alpha, yr, yi, br, bi, 20 * ctx.dof(), tol, x_is_zero=True)
+    assert ok64 and okm
+    st = ctx.stats()
+    assert st.solver_iterations_fp32 == itm
+    # true residual of the mixed solution (oracle operator, FP64)
+    b = (br.cpu().numpy(), bi.cpu().numpy())
+    Ax = om.schro_res(V, alpha, yr.cpu().numpy(), yi.cpu().numpy())
+    r = np.sqrt(om.dot(b[0] - Ax[0], b[0] - Ax[0]) + om.dot(b[1] - Ax[1], b[1] - Ax[1]))
+    bn = np.sqrt(om.dot(b[0], b[0]) + om.dot(b[1], b[1]))
+    assert r < tol * bn + tol
+    # both solutions meet the residual test to 1e-10; they differ by up to
+    # about cond(A) * 1e-10 (the state-level 1e-8 bar is checked per step below)
+    e = max(rel_err(om.unmask(yr.cpu().numpy()), om.unmask(xr.cpu().numpy())),
+            rel_err(om.unmask(yi.cpu().numpy()), om.unmask(xi.cpu().numpy())))
+    assert e < 1e-7
+
+
+def test_diagonal_preconditioner_cuts_inner_iterations(semlib, oracle):
+    from schrodingersem_gb300 import capi
+    ctx, om, re, im, V = _packet_case(semlib, oracle, n=10, p=8)
+    dV = ctx.to_device(V)
+    br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))
+    br.mul_(0.005)
+    bi.mul_(0.005)
+    alpha, tol = 0.005 * 1.0886, 1e-10
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    out = {}
+    for pc in (capi.PRECOND_NONE, capi.PRECOND_DIAG):
+        ctx.set_option(capi.OPT_PRECOND, pc)
+        xr, xi = ctx.zeros(), ctx.zeros()
+        ok, it, res = ctx.minres_schro(dV, alpha, xr, xi, br, bi, 20 * ctx.dof(), tol, x_is_zero=True)
+        assert ok
+        out[pc] = (it, xr.cpu().numpy(), xi.cpu().numpy())
+    assert out[capi.PRECOND_DIAG][0] < 0.7 * out[capi.PRECOND_NONE][0]
+    for k in (1, 2):
+        assert rel_err(om.unmask(out[1][k]), om.unmask(out[0][k])) < 1e-8
+    b = (br.cpu().numpy(), bi.cpu().numpy())
+    Ax = om.schro_res(V, alpha, out[1][1], out[1][2])
+    r = np.sqrt(om.dot(b[0] - Ax[0], b[0] - Ax[0]) + om.dot(b[1] - Ax[1], b[1] - Ax[1]))
+    bn = np.sqrt(om.dot(b[0], b[0]) + om.dot(b[1], b[1]))
+    assert r < tol * bn + tol
+
+
+@pytest.mark.parametrize("method", ["dirk4s3", "bdf2", "dirk4s5"])
+def test_mixed_driver_matches_fp64(semlib, oracle, method):
+    from schrodingersem_gb300 import capi
+    ctx, om, re, im, V = _packet_case(semlib, oracle)
+    T, steps, tol = 0.05, 5, 1e-10
+    a_re, a_im = re.copy(), im.copy()
+    assert ctx.schrodinger(method, a_re, a_im, V, T, T / steps, 20 * ctx.dof(), tol)
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    b_re, b_im = re.copy(), im.copy()
+    rec = []
+    assert ctx.schrodinger(method, b_re, b_im, V, T, T / steps, 20 * ctx.dof(), tol, record=rec)
+    assert len(rec) == steps
+    st = ctx.stats()
+    assert all(st.last_stage_sweeps[k] >= 1 for k in range(st.last_step_stages))
+    assert max(rel_err(b_re, a_re), rel_err(b_im, a_im)) < 1e-8
+
+
+def test_mixed_helmholtz(semlib, oracle, known):
+    from schrodingersem_gb300 import capi
+    p = known["helmholtz_p"]
+    ctx = semlib.Context(p, folder=SMALL_MESH)
+    om = oracle.Mesh(p, folder=SMALL_MESH)
+    X, Y = om.node_coords()
+    f = X * X - Y * Y
+    c = np.full(om.shape, known["helmholtz_c"])
+    u64 = np.zeros(om.shape)
+    assert ctx.helmholtz(u64, c, f, 10 * om.dof(), 1e-10)[0]
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    um = np.zeros(om.shape)
+    assert ctx.helmholtz(um, c, f, 10 * om.dof(), 1e-10)[0]
+    assert rel_err(om.unmask(um), om.unmask(u64)) < 1e-7
