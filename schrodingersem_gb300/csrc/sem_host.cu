@@ -225,6 +225,14 @@ struct sem_ctx {
     double* h_part = nullptr;   // pinned partials for dots
 };
 
+// accessors for the library's other translation units (sem_internal.h)
+namespace semgb {
+const DevMesh& ctx_mesh(const sem_ctx* c) { return c->dm; }
+cudaStream_t ctx_stream(const sem_ctx* c) { return c->stream; }
+void ctx_count_launches(sem_ctx* c, long long k) { c->stats.kernel_launches += k; }
+int ctx_fail(int code, const char* msg) { return fail(code, msg); }
+}  // namespace semgb
+
 static int ctx_alloc(sem_ctx* c, void** p, size_t bytes)
 {
     cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 16));

@@ -153,5 +153,14 @@ cudaError_t launch_solver(const DevMesh& m, const SolveArgs& a, const void* work
 
 }  // namespace semgb
 
+// ---- context accessors (defined in sem_host.cu) ------------------------------
+struct sem_ctx;
+namespace semgb {
+const DevMesh& ctx_mesh(const sem_ctx* c);
+cudaStream_t ctx_stream(const sem_ctx* c);
+void ctx_count_launches(sem_ctx* c, long long k);
+int ctx_fail(int code, const char* msg);  // records the message, returns code
+}  // namespace semgb
+
 #define SEM_FOR_EACH_N(X) \
     X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)

@@ -23,6 +23,8 @@ def main():
     ap.add_argument("--maxit", type=int, default=30)
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--prec", default="fp64", choices=["fp64", "fp32", "mixed"])
+    ap.add_argument("--tol", type=float, default=1e-10, help="0 runs exactly maxit iterations")
+    ap.add_argument("--time", action="store_true", help="print device time per iteration")
     a = ap.parse_args()
     import torch
 
@@ -45,12 +47,20 @@ def main():
         return
     if a.prec == "mixed":
         ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+        ctx.set_option(capi.OPT_INNER_TOL, max(a.tol, 1e-30))
+        ctx.set_option(capi.OPT_MAX_REFINE, 1)
+    ctx.set_option(capi.OPT_PROFILE, 1)
     dV = ctx.to_device(V)
     br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))
-    xr, xi = ctx.zeros(), ctx.zeros()
-    ok, it, res = ctx.minres_schro(dV, 0.0054, xr, xi, br, bi, a.maxit, 1e-10, x_is_zero=True)
-    torch.cuda.synchronize()
-    print(f"minres: success={ok} iterations={it} residual={res:.3e}")
+    for rep in range(a.reps if a.time else 1):
+        xr, xi = ctx.zeros(), ctx.zeros()
+        s0 = ctx.stats()
+        ok, it, res = ctx.minres_schro(dV, 0.0054, xr, xi, br, bi, a.maxit, a.tol, x_is_zero=True)
+        torch.cuda.synchronize()
+        s1 = ctx.stats()
+    ms = s1.solver_kernel_ms - s0.solver_kernel_ms
+    print(f"minres: n={a.n} p={a.p} prec={a.prec} success={ok} iterations={it} residual={res:.3e} "
+          f"kernel_ms={ms:.3f} us_per_iteration={1e3 * ms / max(it, 1):.2f}")
 
 
 if __name__ == "__main__":
