@@ -189,6 +189,22 @@ int sem_apply_schro_f(sem_ctx* ctx, const double* V,
 int sem_apply_schro_res_f32(sem_ctx* ctx, const float* V, float alpha,
                             const float* q_re, const float* q_im, float* out_re, float* out_im);
 
+/* No counterpart in the reference.  The same operator as
+ * sem_apply_schro_res for callers that must not allocate device memory:
+ * code whose device memory is owned and budgeted by a host framework or pool
+ * allocator, and latency-critical loops where the implicit synchronisation of
+ * cudaMalloc/cudaFree is not acceptable.  Its element-local intermediate
+ * lives in a static device array of 2^20 doubles (8 MiB, held by every GPU
+ * that loads the library until exit) instead of a library allocation, so
+ * the call allocates nothing.  Requires 2*E*N*N <= 1048576, otherwise it
+ * returns SEM_ERR_UNSUPPORTED.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * All calls share the array: calls whose kernels overlap on the GPU (other
+ * streams, other contexts) race on it.  Device pointers. */
+int sem_apply_schro_res_noalloc(sem_ctx* ctx, const double* V, double alpha,
+                                const double* q_re, const double* q_im,
+                                double* out_re, double* out_im);
+
 /* --------------------------------------------- Krylov solvers (device) */
 
 /* minres (include/minres.hpp:19-107) on the Schroedinger Res operator with

@@ -67,7 +67,9 @@ SIGNATURES = {
     "sem_apply_helmholtz": (C.c_int, [_vp, _vp, _vp, _vp]),
     "sem_apply_schro_res": (C.c_int, [_vp, _vp, C.c_double, _vp, _vp, _vp, _vp]),
     "sem_apply_schro_f": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
-    "sem_apply_schro_res_f32": (C.c_int, [_vp, _vp, C.c_float, _vp, _vp, _vp, _vp]),    "sem_minres_schro": (C.c_int, [_vp, _vp, C.c_double, _vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int,
+    "sem_apply_schro_res_f32": (C.c_int, [_vp, _vp, C.c_float, _vp, _vp, _vp, _vp]),
+    "sem_apply_schro_res_noalloc": (C.c_int, [_vp, _vp, C.c_double, _vp, _vp, _vp, _vp]),
+    "sem_minres_schro": (C.c_int, [_vp, _vp, C.c_double, _vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int,
                                    C.POINTER(SemSolverResults)]),
     "sem_minres_helmholtz": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.c_int,
                                        C.POINTER(SemSolverResults)]),
