@@ -62,10 +62,15 @@ enum sem_option {
     SEM_OPT_WAIT_TIMEOUT_MS = 4, /* limit of every device-side wait (default 2000 ms) */
     SEM_OPT_MAX_REFINE = 5,      /* cap on FP64 refinement sweeps in mixed mode (default 50) */
     SEM_OPT_PROFILE = 6,         /* 1: time every persistent solver launch with CUDA events */
-    SEM_OPT_PRECOND = 7          /* preconditioner of the FP32 inner solve in mixed mode:
+    SEM_OPT_PRECOND = 7,         /* preconditioner of the FP32 inner solve in mixed mode:
                                     SEM_PRECOND_NONE (default, as the reference) or
                                     SEM_PRECOND_DIAG (diagonal of |A|); the FP64 outer test
                                     on the true residual is unchanged */
+    SEM_OPT_INNER_ITERATION = 8, /* FP32 inner MINRES iteration for Res: 1 (default) one grid
+                                    barrier per iteration (operator product carried by
+                                    recurrence), 0 the two-barrier form of the FP64 solver */
+    SEM_OPT_REFINE_TOL_SCALE = 9 /* mixed mode stops at |r| < s (tol |r0| + tol), s in (0,1],
+                                    default 1 (the reference's test on the true residual) */
 };
 enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
 enum { SEM_PRECOND_NONE = 0, SEM_PRECOND_DIAG = 1 };
@@ -110,6 +115,9 @@ typedef struct {
     double solver_kernel_ms;        /* their summed device time (SEM_OPT_PROFILE only) */
     long long solver_iterations_fp64; /* Krylov iterations run in FP64 */
     long long solver_iterations_fp32; /* Krylov iterations run in FP32 */
+    long long learned_guesses;      /* stage guesses the learned model proposed */
+    long long learned_accepted;     /* ... and that beat the extrapolation's residual */
+    double last_guess_residual_ratio; /* |r(guess used)| / |r(extrapolated)| of the last such stage */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop
@@ -241,6 +249,51 @@ int sem_schrodinger_dirk4s5(sem_ctx* ctx, double* psi_re, double* psi_im, const 
 int sem_schrodinger_dirk4s3(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
                             double T, const sem_solver_opts* opts,
                             sem_step_callback cb, void* user, int* success);
+
+/* ------------------------------------------- learned stage guess (device)
+ * No counterpart in the reference (its stage solves start from zero,
+ * schrodinger.hpp:222,379).  A per-element network predicts the error of the
+ * extrapolated stage guess 2 z^{n-1} - z^{n-2} from that guess's residual.
+ * Rows are elements: input 4 N^2 BF16 features [r_re/s, r_im/s, alpha V,
+ * mass/alpha] with s the element's RMS residual; output 2 N^2 FP32 values,
+ * the correction (z - z_guess)/s.  Network: ReLU MLP d_in -> H -> H -> d_out,
+ * BF16 tensor-core GEMMs with FP32 accumulation, FP32 master weights, Adam.
+ * Weights W are [in][out] row-major FP32. */
+typedef struct sem_learner sem_learner;
+int sem_learner_create(sem_learner** learner, int d_in, int hidden, int d_out,
+                       unsigned long long seed);
+int sem_learner_destroy(sem_learner* learner);
+int sem_learner_shape(const sem_learner* learner, int* d_in, int* hidden, int* d_out);
+int sem_learner_set_stream(sem_learner* learner, void* cuda_stream);
+/* host copies of layer l (0..2) weights [in][out] and biases [out] */
+int sem_learner_get_params(sem_learner* learner, int l, float* W, float* b);
+int sem_learner_set_params(sem_learner* learner, int l, const float* W, const float* b);
+/* out (device FP32, rows x d_out) = network(x), x device BF16 rows x d_in */
+int sem_learner_forward(sem_learner* learner, int rows, const void* x_bf16, float* out);
+/* one batch: loss = mean((net(x) - target)^2) to *loss (host, may be NULL);
+ * gradients kept for sem_learner_get_grads; lr > 0 also takes an Adam step */
+int sem_learner_train_step(sem_learner* learner, int rows, const void* x_bf16,
+                           const float* target, float lr, double* loss);
+int sem_learner_get_grads(sem_learner* learner, int l, float* gW, float* gb);
+/* Adam over `epochs` shuffled passes of minibatches of `batch` rows of a
+ * device dataset (X BF16 rows x d_in, T FP32 rows x d_out) */
+int sem_learner_fit(sem_learner* learner, const void* X, const float* T, long long rows,
+                    int epochs, int batch, float lr, unsigned long long seed, double* final_loss);
+/* C (M x N FP32) = A (M x K BF16) B (K x N BF16), row-major device arrays,
+ * the network's tensor-core GEMM */
+int sem_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, void* cuda_stream);
+/* network used by the SDIRK drivers when SEM_OPT_STAGE_GUESS is
+ * SEM_GUESS_LEARNED in mixed precision (NULL: extrapolation only).  The
+ * caller keeps ownership.  Every proposed guess is checked: the driver keeps
+ * the extrapolation when the network's guess has the larger FP64 residual. */
+int sem_ctx_set_learner(sem_ctx* ctx, sem_learner* learner);
+/* record training rows from the SDIRK drivers' stage solves (mixed precision,
+ * SEM_GUESS_EXTRAPOLATE or _LEARNED, from the third step on) into a device
+ * dataset of capacity_rows rows; 0 stops recording.  Resets the dataset. */
+int sem_ctx_record(sem_ctx* ctx, long long capacity_rows);
+/* the recorded dataset: device pointers X (BF16 rows x d_in), T (FP32 rows x
+ * d_out), rows recorded, d_in = 4 N^2, d_out = 2 N^2 */
+int sem_ctx_dataset(sem_ctx* ctx, void** X, float** T, long long* rows, int* d_in, int* d_out);
 
 #ifdef __cplusplus
 }

@@ -37,7 +37,8 @@ class SemStats(C.Structure):
                 ("last_error_estimate", C.c_double), ("steps_taken", C.c_int),
                 ("kernel_launches", C.c_longlong), ("solver_launches", C.c_longlong),
                 ("solver_kernel_ms", C.c_double), ("solver_iterations_fp64", C.c_longlong),
-                ("solver_iterations_fp32", C.c_longlong)]
+                ("solver_iterations_fp32", C.c_longlong), ("learned_guesses", C.c_longlong),
+                ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double)]
 
 
 STEP_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, _dp, _dp)
@@ -82,11 +83,26 @@ SIGNATURES = {
                                           STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
     "sem_schrodinger_dirk4s3": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(SemSolverOpts),
                                           STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
+    "sem_learner_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int, C.c_int, C.c_ulonglong]),
+    "sem_learner_destroy": (C.c_int, [_vp]),
+    "sem_learner_shape": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "sem_learner_set_stream": (C.c_int, [_vp, _vp]),
+    "sem_learner_get_params": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "sem_learner_set_params": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "sem_learner_forward": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "sem_learner_train_step": (C.c_int, [_vp, C.c_int, _vp, _vp, C.c_float, _dp]),
+    "sem_learner_get_grads": (C.c_int, [_vp, C.c_int, _vp, _vp]),
+    "sem_learner_fit": (C.c_int, [_vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _dp]),
+    "sem_gemm_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
+    "sem_ctx_set_learner": (C.c_int, [_vp, _vp]),
+    "sem_ctx_record": (C.c_int, [_vp, C.c_longlong]),
+    "sem_ctx_dataset": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_longlong),
+                                  C.POINTER(C.c_int), C.POINTER(C.c_int)]),
 }
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
-OPT_PRECOND = 7
+OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE = 7, 8, 9
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG = 0, 1
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

@@ -113,6 +113,32 @@ class Context:
         check(self._L.sem_ctx_get_stats(self._h, C.byref(s)), "stats")
         return s
 
+    # ------------------------------------------------- learned stage guess
+    def set_learner(self, learner):
+        """network for SEM_GUESS_LEARNED (None: extrapolation only); the
+        caller keeps the Learner alive while the context uses it"""
+        self._learner = learner
+        check(self._L.sem_ctx_set_learner(self._h, learner.handle if learner is not None else None),
+              "sem_ctx_set_learner")
+
+    def record(self, capacity_rows: int):
+        """start recording training rows from the SDIRK stage solves"""
+        check(self._L.sem_ctx_record(self._h, C.c_longlong(int(capacity_rows))), "sem_ctx_record")
+
+    def dataset(self):
+        """copies of the recorded rows: (X bf16 (rows, 4N^2), T float32 (rows, 2N^2))"""
+        from .learned import device_view
+        torch = _torch()
+        X, T = C.c_void_p(), C.c_void_p()
+        rows, di, do = C.c_longlong(0), C.c_int(0), C.c_int(0)
+        check(self._L.sem_ctx_dataset(self._h, C.byref(X), C.byref(T), C.byref(rows), C.byref(di), C.byref(do)),
+              "sem_ctx_dataset")
+        torch.cuda.current_stream().synchronize()
+        r = int(rows.value)
+        Xv = device_view(X.value or 0, (r, di.value), torch.bfloat16).clone()
+        Tv = device_view(T.value or 0, (r, do.value), torch.float32).clone()
+        return Xv, Tv
+
     # ------------------------------------------------------- device helpers
     def zeros(self, dtype=None, planes: int = 1):
         torch = _torch()

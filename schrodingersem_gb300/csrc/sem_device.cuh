@@ -418,31 +418,32 @@ __device__ __forceinline__ unsigned long long global_ns()
     return t;
 }
 
-// Grid-wide barrier for cooperatively launched kernels.  Every wait is
-// bounded: after timeout_ns the block records gs->err and returns false, so
-// no block can spin forever.  Returns true when all blocks arrived.
+// Grid-wide barrier for cooperatively launched kernels.  One atomic per block:
+// block 0 adds 2^31 - (G-1), every other block adds 1, so the counter's top
+// bit flips exactly when the last block arrives and its low bits return to
+// their start value (gs->count starts at 0).  Every wait is bounded: after
+// timeout_ns the block records gs->err and returns false, so no block can spin
+// forever.  Returns true when all blocks arrived.
 __device__ __forceinline__ bool grid_barrier(GridSync* gs, long long timeout_ns)
 {
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned int* vgen = &gs->gen;
+        const unsigned int inc = (blockIdx.x == 0) ? (0x80000000u - (gridDim.x - 1)) : 1u;
+        volatile unsigned int* vc = &gs->count;
         volatile int* verr = &gs->err;
-        const unsigned int g = *vgen;
         __threadfence();
-        const unsigned int arrived = atomicAdd(&gs->count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&gs->count, 0u);
-            __threadfence();
-            atomicAdd(&gs->gen, 1u);
-        } else {
+        const unsigned int old = atomicAdd(&gs->count, inc);
+        if (((old ^ *vc) & 0x80000000u) == 0) {
             const unsigned long long t0 = global_ns();
-            while (*vgen == g) {
-                if (*verr) break;
-                if ((long long)(global_ns() - t0) > timeout_ns) {
-                    atomicExch(&gs->err, 1);
-                    break;
+            unsigned int polls = 0;
+            while (((old ^ *vc) & 0x80000000u) == 0) {
+                if ((++polls & 63u) == 0) {
+                    if (*verr) break;
+                    if ((long long)(global_ns() - t0) > timeout_ns) {
+                        atomicExch(&gs->err, 1);
+                        break;
+                    }
                 }
-                __nanosleep(64);
             }
         }
         __threadfence();
@@ -458,11 +459,14 @@ __device__ __forceinline__ double grid_sum(double v, double* partials, int slot,
 {
     const double bs = block_sum(v, red);
     const int G = gridDim.x;
-    if (threadIdx.x == 0) partials[(size_t)slot * G + blockIdx.x] = bs;
+    // same slot layout as grid_sum2 ([slot][2][grid]) so that consecutive
+    // reductions (alternating slots) never share partial-sum words
+    double* p = partials + (size_t)(2 * slot) * G;
+    if (threadIdx.x == 0) p[blockIdx.x] = bs;
     ok = grid_barrier(gs, timeout_ns);
     if (threadIdx.x < 32) {
         double s = 0.0;
-        for (int q = threadIdx.x; q < G; q += 32) s += __ldcg(partials + (size_t)slot * G + q);
+        for (int q = threadIdx.x; q < G; q += 32) s += __ldcg(p + q);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (threadIdx.x == 0) red[33] = s;
@@ -471,6 +475,43 @@ __device__ __forceinline__ double grid_sum(double v, double* partials, int slot,
     const double r = red[33];
     __syncthreads();
     return r;
+}
+
+// all-reduce of two doubles behind a single grid barrier; partials laid out
+// [slot][2][grid] (the buffer holds 2 slots x 2 values x grid)
+__device__ __forceinline__ void grid_sum2(double v0, double v1, double* partials, int slot, GridSync* gs,
+                                          long long timeout_ns, double* red, bool& ok, double& r0, double& r1)
+{
+    const double b0 = block_sum(v0, red);
+    const double b1 = block_sum(v1, red);
+    const int G = gridDim.x;
+    double* p0 = partials + (size_t)(slot * 2) * G;
+    double* p1 = p0 + G;
+    if (threadIdx.x == 0) {
+        p0[blockIdx.x] = b0;
+        p1[blockIdx.x] = b1;
+    }
+    ok = grid_barrier(gs, timeout_ns);
+    if (threadIdx.x < 32) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int q = threadIdx.x; q < G; q += 32) {
+            s0 += __ldcg(p0 + q);
+            s1 += __ldcg(p1 + q);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        }
+        if (threadIdx.x == 0) {
+            red[33] = s0;
+            red[32] = s1;
+        }
+    }
+    __syncthreads();
+    r0 = red[33];
+    r1 = red[32];
+    __syncthreads();
 }
 
 }  // namespace semgb

@@ -216,6 +216,16 @@ struct sem_ctx {
     int max_refine = 50;
     bool profile = false;
     int precond = 0;
+    int inner_fused = 1;
+    double outer_scale = 1.0;
+    // stage-guess history of the SDIRK drivers (persists across calls)
+    long long hist_steps = 0;
+    int hist_stages = 0;
+    double hist_dt = 0.0;
+    // learned stage guess: network (owned by the caller) and the training
+    // dataset recorded from solved stages (device workspace ds_X, ds_T)
+    sem_learner* learner = nullptr;
+    long long ds_cap = 0, ds_rows = 0;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     sem_stats stats{};
     // workspace
@@ -638,6 +648,7 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
             if (v != SEM_GUESS_ZERO && v != SEM_GUESS_EXTRAPOLATE && v != SEM_GUESS_LEARNED)
                 return fail(SEM_ERR_ARG, "bad guess mode");
             c->guess = (int)v;
+            c->hist_steps = 0;  // a new guess mode starts a new history
             return SEM_OK;
         case SEM_OPT_WAIT_TIMEOUT_MS:
             if (!(v > 0)) return fail(SEM_ERR_ARG, "timeout must be positive");
@@ -646,6 +657,14 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_MAX_REFINE:
             if (!(v >= 1)) return fail(SEM_ERR_ARG, "max refine must be >= 1");
             c->max_refine = (int)v;
+            return SEM_OK;
+        case SEM_OPT_REFINE_TOL_SCALE:
+            if (!(v > 0 && v <= 1)) return fail(SEM_ERR_ARG, "refinement tolerance scale must be in (0,1]");
+            c->outer_scale = v;
+            return SEM_OK;
+        case SEM_OPT_INNER_ITERATION:
+            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "inner iteration must be 0 or 1");
+            c->inner_fused = (int)v;
             return SEM_OK;
         case SEM_OPT_PRECOND:
             if (v != SEM_PRECOND_NONE && v != SEM_PRECOND_DIAG) return fail(SEM_ERR_ARG, "bad preconditioner");
@@ -912,7 +931,7 @@ static int finish_solve(sem_ctx* c, SolveOut* out, GridSync* sync, sem_solver_re
 // FP64 refinement around an FP32 inner MINRES (SEM_PREC_MIXED)
 static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
                      const double* const b[2], int maxit, double tol, int x_is_zero,
-                     sem_solver_results* res, int* sweeps)
+                     sem_solver_results* res, int* sweeps, int rel_to_b)
 {
     const int nc = (op == OP_RES) ? 2 : 1;
     const size_t v = (size_t)nc * c->n;
@@ -948,6 +967,11 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     }
     mx.pot32 = pot32;
     mx.pinv32 = nullptr;
+    mx.fused = c->inner_fused;
+    mx.outer_scale = c->outer_scale;
+    if (c->inner_fused) {
+        if ((s = wsget(c, "k32_AZ", v, &w.AZ)) || (s = wsget(c, "k32_Y3", v, &w.Y3))) return s;
+    }
     if (c->precond) {
         float* pinv = nullptr;
         if ((s = wsget(c, "mx_pinv32", c->n, &pinv))) return s;
@@ -976,6 +1000,7 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     a.maxit = maxit;
     a.tol = tol;
     a.x_is_zero = x_is_zero;
+    a.rel_to_b = rel_to_b;
     a.timeout_ns = (long long)(c->timeout_ms * 1e6);
     a.sync = sync;
     a.out = out;
@@ -999,12 +1024,12 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
 
 static int run_krylov(sem_ctx* c, int op, const double* pot, double alpha, double* const x[2],
                       const double* const b[2], int maxit, double tol, int x_is_zero,
-                      sem_solver_results* res, int* sweeps = nullptr)
+                      sem_solver_results* res, int* sweeps = nullptr, int rel_to_b = 0)
 {
     if (sweeps) *sweeps = 1;
     if (c->prec == SEM_PREC_MIXED && op != OP_LAPLACE) {
         int sw = 0;
-        int s = run_mixed(c, op, pot, alpha, x, b, maxit, tol, x_is_zero, res, &sw);
+        int s = run_mixed(c, op, pot, alpha, x, b, maxit, tol, x_is_zero, res, &sw, rel_to_b);
         if (sweeps) *sweeps = sw;
         return s;
     }
@@ -1215,7 +1240,172 @@ static int schro_stage_solve(SchroRun* r, double alpha, const double* b, double*
     sem_ctx* c = r->c;
     double* x[2] = {z, z + c->n};
     const double* bb[2] = {b, b + c->n};
-    return run_krylov(c, OP_RES, r->V, alpha, x, bb, max_iter, tol, x_is_zero, res, sweeps);
+    // a warm-started stage is judged relative to |b|, which is the
+    // reference's test (relative to |r_0| = |b|) for the zero start
+    return run_krylov(c, OP_RES, r->V, alpha, x, bb, max_iter, tol, x_is_zero, res, sweeps, !x_is_zero);
+}
+
+// ------------------------------------------------------ learned stage guess
+static int launch_learn_op(sem_ctx* c, const LearnArgs& a)
+{
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) { return launch_learn<decltype(nv)::value>(c->dm, a, c->stream); }));
+    return SEM_OK;
+}
+
+// r = b - A z (continuous format, two planes) for a guess z
+static int guess_residual(sem_ctx* c, const double* V, double alpha, const double* b, const double* z, double* r)
+{
+    double* Y = nullptr;
+    int s = wsget(c, "lr_Y", 2 * c->n, &Y);
+    if (s) return s;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_apply<decltype(nv)::value>(c->dm, OP_RES, false, V, alpha, z, z + c->n, Y, Y + c->n, true,
+                                                 c->stream);
+    }));
+    LearnArgs a{};
+    a.what = LEARN_RESID;
+    a.b = b;
+    a.Y = Y;
+    a.r = r;
+    c->stats.fp64_applies++;
+    return launch_learn_op(c, a);
+}
+
+static int norm2_planes(sem_ctx* c, const double* r, double* out)
+{
+    double a1 = 0, a2 = 0;
+    int s = 0;
+    if ((s = dot_dev(c, r, r, &a1)) || (s = dot_dev(c, r + c->n, r + c->n, &a2))) return s;
+    *out = a1 + a2;
+    return SEM_OK;
+}
+
+// Build the per-element features of the extrapolated guess z (its scaled
+// residual, alpha V, mass / alpha); with `use`, let the network predict a
+// correction and keep it only if its FP64 residual is smaller than the
+// extrapolation's (the extrapolation stays the fallback).  *zext receives a
+// copy of the extrapolated guess (the base the targets are measured from).
+static int learned_guess(sem_ctx* c, const double* V, double alpha, const double* b, double* z, bool use,
+                         double** zext)
+{
+    const int NN = c->N * c->N;
+    double *r = nullptr, *zx = nullptr;
+    void* x = nullptr;
+    float* sig = nullptr;
+    int s = 0;
+    if ((s = wsget(c, "lr_r", 2 * c->n, &r)) || (s = wsget(c, "lr_zext", 2 * c->n, &zx)) ||
+        (s = wsbuf(c, "lr_x", (size_t)c->E * 4 * NN * 2, &x)) || (s = wsget(c, "lr_sig", c->E, &sig)))
+        return s;
+    SEM_CUDA(cudaMemcpyAsync(zx, z, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    *zext = zx;
+    if ((s = guess_residual(c, V, alpha, b, zx, r))) return s;
+    LearnArgs a{};
+    a.what = LEARN_FEATURES;
+    a.r = r;
+    a.V = V;
+    a.alpha = alpha;
+    a.x = x;
+    a.sigma = sig;
+    if ((s = launch_learn_op(c, a))) return s;
+    if (!use) return SEM_OK;
+    float* delta = nullptr;
+    double *zl = nullptr, *r2 = nullptr;
+    if ((s = wsget(c, "lr_delta", (size_t)c->E * 2 * NN, &delta)) || (s = wsget(c, "lr_zl", 2 * c->n, &zl)) ||
+        (s = wsget(c, "lr_r2", 2 * c->n, &r2)))
+        return s;
+    if ((s = sem_learner_set_stream(c->learner, c->stream)) || (s = sem_learner_forward(c->learner, c->E, x, delta)))
+        return s;
+    LearnArgs k{};
+    k.what = LEARN_CORRECT;
+    k.zg = zx;
+    k.sigma = sig;
+    k.delta = delta;
+    k.zo = zl;
+    if ((s = launch_learn_op(c, k))) return s;
+    if ((s = guess_residual(c, V, alpha, b, zl, r2))) return s;
+    double n_ext = 0, n_l = 0;
+    if ((s = norm2_planes(c, r, &n_ext)) || (s = norm2_planes(c, r2, &n_l))) return s;
+    c->stats.learned_guesses++;
+    if (n_l < n_ext) {
+        SEM_CUDA(cudaMemcpyAsync(z, zl, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+        c->stats.learned_accepted++;
+    }
+    c->stats.last_guess_residual_ratio = n_ext > 0 ? std::sqrt(std::min(n_l, n_ext) / n_ext) : 1.0;
+    return SEM_OK;
+}
+
+// append (features, (z - zext)/sigma) of every element to the dataset
+static int record_sample(sem_ctx* c, const double* z, const double* zext)
+{
+    const int NN = c->N * c->N;
+    if (c->ds_rows + c->E > c->ds_cap) return SEM_OK;  // full: keep the first samples
+    void* x = nullptr;
+    float *sig = nullptr, *t = nullptr;
+    int s = 0;
+    if ((s = wsbuf(c, "lr_x", (size_t)c->E * 4 * NN * 2, &x)) || (s = wsget(c, "lr_sig", c->E, &sig)) ||
+        (s = wsget(c, "lr_t", (size_t)c->E * 2 * NN, &t)))
+        return s;
+    LearnArgs a{};
+    a.what = LEARN_TARGETS;
+    a.z = z;
+    a.zg = zext;
+    a.sigma = sig;
+    a.t = t;
+    if ((s = launch_learn_op(c, a))) return s;
+    void* dX = nullptr;
+    float* dT = nullptr;
+    if ((s = wsbuf(c, "ds_X", (size_t)c->ds_cap * 4 * NN * 2, &dX)) ||
+        (s = wsget(c, "ds_T", (size_t)c->ds_cap * 2 * NN, &dT)))
+        return s;
+    SEM_CUDA(cudaMemcpyAsync((char*)dX + (size_t)c->ds_rows * 4 * NN * 2, x, (size_t)c->E * 4 * NN * 2,
+                             cudaMemcpyDeviceToDevice, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(dT + (size_t)c->ds_rows * 2 * NN, t, (size_t)c->E * 2 * NN * sizeof(float),
+                             cudaMemcpyDeviceToDevice, c->stream));
+    c->ds_rows += c->E;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_set_learner(sem_ctx* c, sem_learner* L)
+{
+    SEM_CHECK_CTX(c);
+    if (L) {
+        int din = 0, dout = 0;
+        int s = sem_learner_shape(L, &din, nullptr, &dout);
+        if (s) return s;
+        if (din != 4 * c->N * c->N || dout != 2 * c->N * c->N)
+            return fail(SEM_ERR_ARG, "learner shape must be 4 N^2 -> 2 N^2 for this mesh");
+    }
+    c->learner = L;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_record(sem_ctx* c, long long capacity_rows)
+{
+    SEM_CHECK_CTX(c);
+    if (capacity_rows < 0) return fail(SEM_ERR_ARG, "negative capacity");
+    c->ds_cap = capacity_rows;
+    c->ds_rows = 0;
+    return SEM_OK;
+}
+
+extern "C" int sem_ctx_dataset(sem_ctx* c, void** X, float** T, long long* rows, int* d_in, int* d_out)
+{
+    SEM_CHECK_CTX(c);
+    const int NN = c->N * c->N;
+    if (d_in) *d_in = 4 * NN;
+    if (d_out) *d_out = 2 * NN;
+    if (rows) *rows = c->ds_rows;
+    void* dX = nullptr;
+    float* dT = nullptr;
+    if (c->ds_cap > 0) {
+        int s = 0;
+        if ((s = wsbuf(c, "ds_X", (size_t)c->ds_cap * 4 * NN * 2, &dX)) ||
+            (s = wsget(c, "ds_T", (size_t)c->ds_cap * 2 * NN, &dT)))
+            return s;
+    }
+    if (X) *X = dX;
+    if (T) *T = dT;
+    return SEM_OK;
 }
 
 static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, const double* V,
@@ -1248,9 +1438,22 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
         bw = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0, 0.25};
         ew = {-3.0 / 16.0, -27.0 / 32.0, 25.0 / 32.0, 0.0, 0.25};
     }
+    // stage solutions of the current and the two previous steps (ring of 3)
+    const size_t zset = (size_t)stages * 2 * c->n;
+    const bool extrap = (c->guess == SEM_GUESS_EXTRAPOLATE || c->guess == SEM_GUESS_LEARNED) &&
+                        c->prec == SEM_PREC_MIXED;
+    // the stage history carries over from the previous driver call when it
+    // continued the same kind of step (a wrong history only costs iterations:
+    // every stage is still solved to the same tolerance)
+    if (!extrap || c->hist_stages != stages || c->hist_dt != o->dt) c->hist_steps = 0;
+    c->hist_stages = stages;
+    c->hist_dt = o->dt;
+    const long long hist0 = c->hist_steps;
+    double* Zring = nullptr;
     double* Z = nullptr;
     double* b = nullptr;
-    if ((s = wsget(c, "drv_Z", (size_t)stages * 2 * c->n, &Z))) return s;
+    if ((s = wsget(c, "drv_Z", (extrap ? 3 : 1) * zset, &Zring))) return s;
+    Z = Zring;
     if ((s = wsget(c, "drv_b2", 2 * c->n, &b))) return s;
     double pnorm = 0.0;
     if (stages == 5) {
@@ -1263,6 +1466,8 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
     int step = 0;
     while (t < T) {  // schrodinger.hpp:219, 376
         c->stats.last_step_stages = stages;
+        const long long gstep = hist0 + step;  // steps of this trajectory so far
+        if (extrap) Z = Zring + (size_t)(gstep % 3) * zset;
         for (int st = 0; st < stages; ++st) {
             ZList zl{};
             zl.nz = st;
@@ -1272,18 +1477,48 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             }
             if ((s = schro_rhs(&r, o->dt, zl, b))) return s;
             double* z = Z + (size_t)st * 2 * c->n;
-            SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
+            // initial guess: zero as the reference (schrodinger.hpp:222,379), or
+            // the stage's solution extrapolated linearly from the last two steps
+            int x_zero = 1;
+            if (extrap && gstep >= 1) {
+                const double* z1 = Zring + (size_t)((gstep - 1) % 3) * zset + (size_t)st * 2 * c->n;
+                if (gstep >= 2) {
+                    const double* z2 = Zring + (size_t)((gstep - 2) % 3) * zset + (size_t)st * 2 * c->n;
+                    k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, 2.0, z1, -1.0, z2, z);
+                    c->stats.kernel_launches++;
+                    SEM_CUDA(cudaGetLastError());
+                } else {
+                    SEM_CUDA(cudaMemcpyAsync(z, z1, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+                }
+                x_zero = 0;
+            } else {
+                SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
+            }
+            // learned correction of the extrapolated guess, and/or a training
+            // sample (the guess's residual features; its error after the solve)
+            const bool rec = extrap && gstep >= 2 && c->ds_cap > 0;
+            const bool use = extrap && gstep >= 2 && c->guess == SEM_GUESS_LEARNED && c->learner;
+            double* zext = nullptr;
+            if (rec || use) {
+                if ((s = learned_guess(c, r.V, alpha, b, z, use, &zext))) return s;
+            }
             sem_solver_results res{};
             int sw = 1;
-            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, 1, &res, &sw))) return s;
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw))) return s;
             c->stats.last_stage_iters[st] = res.n_iter;
             c->stats.last_stage_sweeps[st] = sw;
+            if (rec && res.success) {
+                if ((s = record_sample(c, z, zext))) return s;
+            }
             if (!res.success) {
                 ok = false;
                 break;
             }
         }
-        if (!ok) break;
+        if (!ok) {
+            c->hist_steps = 0;
+            break;
+        }
         ZList zb{};
         zb.nz = stages;
         for (int l = 0; l < stages; ++l) {
@@ -1313,6 +1548,7 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
         }
         t += o->dt;
         ++step;
+        c->hist_steps = hist0 + step;
         c->stats.steps_taken = step;
         if (cb) {
             if ((s = schro_publish(&r))) return s;

@@ -79,6 +79,8 @@ struct KrylovWork {
     T* W[3];        // MINRES direction vectors / PCG p, r
     T* Y[2];        // element-local operator output
     double* partials;  // [2 slots][grid][4]
+    T* AZ;          // single-barrier MINRES: assembled A z_i (continuous format)
+    T* Y3;          // single-barrier MINRES: y_i before the r2 correction
 };
 
 struct SolveArgs {
@@ -92,6 +94,8 @@ struct SolveArgs {
     double tol;
     int x_is_zero;
     int kmax;         // elements staged per pass (solver_plan)
+    int rel_to_b;     // mixed solver: stop on |r| < tol |b| + tol instead of tol |r_0| + tol
+                      // (the same test when x_0 = 0; used with warm starts)
     long long timeout_ns;
     GridSync* sync;
     SolveOut* out;
@@ -108,6 +112,8 @@ struct MixedArgs {
     float* x32[2];       // FP32 correction planes
     const float* pot32;  // FP32 copy of the potential (V or c)
     const float* pinv32; // diagonal preconditioner P^-1 (continuous format), or null
+    int fused;           // inner solve with the single-barrier MINRES iteration (Res only)
+    double outer_scale;  // refinement stops at |r| < outer_scale * (tol |r0| + tol)
 };
 
 // ---- launchers, one explicit instantiation per N in sem_inst.cu -------------
@@ -140,6 +146,25 @@ cudaError_t launch_combo_f(const DevMesh& m, const double* V, const double* p, c
 template <int N>
 cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl, double* p_out,
                           cudaStream_t st);
+// per-element kernels of the learned stage guess (see k_features)
+enum LearnWhat : int { LEARN_RESID = 0, LEARN_FEATURES = 1, LEARN_TARGETS = 2, LEARN_CORRECT = 3 };
+struct LearnArgs {
+    int what;
+    const double* b;      // RESID: right-hand side (masked), 2 planes
+    const double* Y;      // RESID: element-local operator output of the guess, 2 planes
+    double* r;            // RESID out / FEATURES in: residual (continuous), 2 planes
+    const double* V;      // FEATURES: potential
+    double alpha;         // FEATURES: stage coefficient
+    void* x;              // FEATURES out: BF16 rows [E][4 N^2]
+    float* sigma;         // FEATURES out / TARGETS, CORRECT in: per-element scale
+    const double* z;      // TARGETS: converged stage solution
+    const double* zg;     // TARGETS, CORRECT: the guess it started from
+    float* t;             // TARGETS out: FP32 rows [E][2 N^2]
+    const float* delta;   // CORRECT: predicted rows [E][2 N^2]
+    double* zo;           // CORRECT out: corrected guess
+};
+template <int N>
+cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st);
 // persistent Krylov solvers (cooperative launch).  solver_plan picks the grid
 // (at most one block per SM) and the per-pass staging capacity in elements;
 // launch_solver runs MINRES (op OP_RES/OP_HELM), PCG (OP_LAPLACE) or, when

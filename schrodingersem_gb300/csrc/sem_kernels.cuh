@@ -2,6 +2,7 @@
 // combinations) and their launchers.  Included by the sem_inst_*.cu units,
 // which instantiate them for a list of polynomial degrees.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 #include "sem_device.cuh"
@@ -145,6 +146,105 @@ __global__ void k_update(DevMesh m, const double* __restrict__ p_in, ZList zl,
     }
 }
 
+// ------------------------------------------------- learned stage guess
+// r = unmask(b) - DSS_cont(Y) for two planes: the residual of a guess whose
+// element-local operator output is Y, in the continuous format
+template <int N>
+__global__ void k_resid_cont(DevMesh m, const double* __restrict__ b, const double* __restrict__ Y,
+                             double* __restrict__ r)
+{
+    constexpr int NN = N * N;
+    const long long n = m.n;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(idx / NN);
+        const int node = (int)(idx - (long long)e * NN);
+        const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+        const long long src = ni_gather_src(m, ni, e, idx);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) r[q * n + idx] = b[q * n + src] - dss_value<N, double, DSS_CONT>(m, Y + q * n, ni, e, idx);
+    }
+}
+
+// One warp per element.  sigma_e = RMS of the residual over the element's
+// nodes (both planes); features (BF16, row e):
+//   [r_re / sigma, r_im / sigma, alpha V, (w_i w_j J) / alpha]   (4 N^2 values)
+template <int N>
+__global__ void k_features(DevMesh m, const double* __restrict__ r, const double* __restrict__ V, double alpha,
+                           __nv_bfloat16* __restrict__ x, float* __restrict__ sigma)
+{
+    constexpr int NN = N * N;
+    const long long n = m.n;
+    const int e = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (e >= m.E) return;
+    const long long base = (long long)e * NN;
+    double s = 0.0;
+    for (int k = lane; k < NN; k += 32) {
+        const double a = r[base + k], b = r[n + base + k];
+        s += a * a + b * b;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    const double sg = sqrt(s / (2.0 * NN)) + 1e-300;
+    const double inv = 1.0 / sg;
+    __nv_bfloat16* row = x + (long long)e * 4 * NN;
+    for (int k = lane; k < NN; k += 32) {
+        row[k] = __float2bfloat16((float)(r[base + k] * inv));
+        row[NN + k] = __float2bfloat16((float)(r[n + base + k] * inv));
+        row[2 * NN + k] = __float2bfloat16((float)(alpha * V[base + k]));
+        row[3 * NN + k] = __float2bfloat16((float)(m.mass[base + k] / alpha));
+    }
+    if (lane == 0) sigma[e] = (float)sg;
+}
+
+// training target of element e: (z - z_guess) / sigma_e at every node, with
+// the solution read at the owner copies (continuous values)
+template <int N>
+__global__ void k_targets(DevMesh m, const double* __restrict__ z, const double* __restrict__ zg,
+                          const float* __restrict__ sigma, float* __restrict__ t)
+{
+    constexpr int NN = N * N;
+    const long long n = m.n;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(idx / NN);
+        const int node = (int)(idx - (long long)e * NN);
+        const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+        const long long src = ni_gather_src(m, ni, e, idx);
+        const double inv = 1.0 / (double)sigma[e];
+        float* row = t + (long long)e * 2 * NN;
+        row[node] = (float)((z[src] - zg[src]) * inv);
+        row[NN + node] = (float)((z[n + src] - zg[n + src]) * inv);
+    }
+}
+
+// z_out = z_guess + sigma_e * delta_e in the masked format: the owner copy
+// of each node takes its element's correction, other copies and the
+// boundary stay zero (z_guess is masked)
+template <int N>
+__global__ void k_correct(DevMesh m, const double* __restrict__ zg, const float* __restrict__ sigma,
+                          const float* __restrict__ delta, double* __restrict__ zo)
+{
+    constexpr int NN = N * N;
+    const long long n = m.n;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(idx / NN);
+        const int node = (int)(idx - (long long)e * NN);
+        const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+        if (!ni_owner(ni) || ni_boundary(ni)) {
+            zo[idx] = 0.0;
+            zo[n + idx] = 0.0;
+            continue;
+        }
+        const double s = (double)sigma[e];
+        const float* row = delta + (long long)e * 2 * NN;
+        zo[idx] = zg[idx] + s * (double)row[node];
+        zo[n + idx] = zg[n + idx] + s * (double)row[NN + node];
+    }
+}
+
 // ------------------------------------------------------------- launchers
 
 inline int grid_for(long long work, int tpb, int cap = 152 * 32)
@@ -257,6 +357,22 @@ cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl,
     return cudaGetLastError();
 }
 
+template <int N>
+cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
+{
+    const int grid = grid_for(m.n, 256);
+    switch (a.what) {
+        case LEARN_RESID: k_resid_cont<N><<<grid, 256, 0, st>>>(m, a.b, a.Y, a.r); break;
+        case LEARN_FEATURES:
+            k_features<N><<<(m.E + 7) / 8, 256, 0, st>>>(m, a.r, a.V, a.alpha, (__nv_bfloat16*)a.x, a.sigma);
+            break;
+        case LEARN_TARGETS: k_targets<N><<<grid, 256, 0, st>>>(m, a.z, a.zg, a.sigma, a.t); break;
+        case LEARN_CORRECT: k_correct<N><<<grid, 256, 0, st>>>(m, a.zg, a.sigma, a.delta, a.zo); break;
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
 }  // namespace semgb
 
 #define SEM_INSTANTIATE(NV)                                                                          \
@@ -275,6 +391,7 @@ cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl,
     template cudaError_t launch_update<NV>(const DevMesh&, const double*, const ZList&, double*,     \
                                            cudaStream_t);                                            \
     template int solver_plan<NV>(int, bool, int, int, size_t, int*, size_t*);                        \
+    template cudaError_t launch_learn<NV>(const DevMesh&, const LearnArgs&, cudaStream_t);           \
     template cudaError_t launch_solver<NV>(const DevMesh&, const SolveArgs&, const void*,            \
                                            const MixedArgs*, int, size_t, cudaStream_t);             \
     }

@@ -1,0 +1,547 @@
+// Learned initial guess for the implicit stage solves: a per-element MLP
+// (BF16 weights and activations on the tensor cores, FP32 accumulation,
+// FP32 master weights and Adam state) trained on the GPU with this file's
+// own forward and backward kernels.
+//
+// Model: x (d_in) -> ReLU(x W1 + b1) (H) -> ReLU(. W2 + b2) (H) -> . W3 + b3 (d_out)
+// with row-major activations [rows][features] and weights [in][out].
+//
+// GEMM: C[M][N] = A(M x K) * B(K x N) with generic strides, tiles of 64 x 64
+// staged in shared memory as BF16, computed with mma.sync m16n8k16 (BF16 in,
+// FP32 accumulate); every global access is bounds-checked.
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sem_gb300.h"
+#include "sem_device.cuh"
+#include "sem_internal.h"
+
+using namespace semgb;
+
+namespace {
+
+constexpr int GT_M = 64, GT_N = 64, GT_K = 32;
+
+struct GemmArgs {
+    int M, N, K;
+    const void* A;
+    long long sa_m, sa_k;  // A(m,k) = A[m*sa_m + k*sa_k]
+    int a_bf16;            // A is __nv_bfloat16 (else float)
+    const void* B;
+    long long sb_k, sb_n;  // B(k,n) = B[k*sb_k + n*sb_n]
+    int b_bf16;
+    float* C;              // C[m*ldc + n] (FP32)
+    int ldc;
+    const float* bias;     // optional, length N
+    int relu;              // ReLU epilogue
+    int accumulate;        // C += result
+    __nv_bfloat16* Cbf;    // optional BF16 copy of the output
+};
+
+__device__ __forceinline__ float ld_any(const void* p, long long i, int bf)
+{
+    return bf ? __bfloat162float(((const __nv_bfloat16*)p)[i]) : ((const float*)p)[i];
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(__nv_bfloat16 lo, __nv_bfloat16 hi)
+{
+    return (uint32_t)__bfloat16_as_ushort(lo) | ((uint32_t)__bfloat16_as_ushort(hi) << 16);
+}
+
+// 128 threads = 4 warps in a 2 x 2 arrangement, each warp 32 x 32 of C
+__global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g)
+{
+    // A tile [64][32] and B tile transposed [64 n][32 k], BF16, padded rows
+    __shared__ __nv_bfloat16 sA[GT_M][GT_K + 8];
+    __shared__ __nv_bfloat16 sB[GT_N][GT_K + 8];
+    const int m0 = blockIdx.y * GT_M, n0 = blockIdx.x * GT_N;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wm = (warp >> 1) * 32, wn = (warp & 1) * 32;
+    float acc[2][4][4];
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) acc[a][b][c] = 0.f;
+    const int gq = lane >> 2, tq = lane & 3;  // mma fragment coordinates
+    for (int k0 = 0; k0 < g.K; k0 += GT_K) {
+        for (int t = threadIdx.x; t < GT_M * GT_K; t += blockDim.x) {
+            const int r = t / GT_K, c = t - r * GT_K;
+            const int m = m0 + r, k = k0 + c;
+            const float v = (m < g.M && k < g.K) ? ld_any(g.A, m * g.sa_m + k * g.sa_k, g.a_bf16) : 0.f;
+            sA[r][c] = __float2bfloat16(v);
+        }
+        for (int t = threadIdx.x; t < GT_N * GT_K; t += blockDim.x) {
+            const int r = t / GT_K, c = t - r * GT_K;  // r: n, c: k
+            const int n = n0 + r, k = k0 + c;
+            const float v = (n < g.N && k < g.K) ? ld_any(g.B, k * g.sb_k + n * g.sb_n, g.b_bf16) : 0.f;
+            sB[r][c] = __float2bfloat16(v);
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < GT_K; kk += 16) {
+            uint32_t af[2][4], bfr[4][2];
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const int r = wm + a * 16 + gq;
+                af[a][0] = pack_bf16(sA[r][kk + 2 * tq], sA[r][kk + 2 * tq + 1]);
+                af[a][1] = pack_bf16(sA[r + 8][kk + 2 * tq], sA[r + 8][kk + 2 * tq + 1]);
+                af[a][2] = pack_bf16(sA[r][kk + 2 * tq + 8], sA[r][kk + 2 * tq + 9]);
+                af[a][3] = pack_bf16(sA[r + 8][kk + 2 * tq + 8], sA[r + 8][kk + 2 * tq + 9]);
+            }
+#pragma unroll
+            for (int b = 0; b < 4; ++b) {
+                const int nn = wn + b * 8 + gq;
+                bfr[b][0] = pack_bf16(sB[nn][kk + 2 * tq], sB[nn][kk + 2 * tq + 1]);
+                bfr[b][1] = pack_bf16(sB[nn][kk + 2 * tq + 8], sB[nn][kk + 2 * tq + 9]);
+            }
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b = 0; b < 4; ++b)
+                    asm volatile(
+                        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+                        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+                        : "+f"(acc[a][b][0]), "+f"(acc[a][b][1]), "+f"(acc[a][b][2]), "+f"(acc[a][b][3])
+                        : "r"(af[a][0]), "r"(af[a][1]), "r"(af[a][2]), "r"(af[a][3]), "r"(bfr[b][0]),
+                          "r"(bfr[b][1]));
+        }
+        __syncthreads();
+    }
+    // epilogue: fragment (row gq / gq+8, cols 2tq, 2tq+1)
+#pragma unroll
+    for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b)
+#pragma unroll
+            for (int h = 0; h < 2; ++h)
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    const int m = m0 + wm + a * 16 + gq + h * 8;
+                    const int nn = n0 + wn + b * 8 + 2 * tq + q;
+                    if (m >= g.M || nn >= g.N) continue;
+                    float v = acc[a][b][h * 2 + q];
+                    if (g.accumulate) v += g.C[(long long)m * g.ldc + nn];
+                    if (g.bias) v += g.bias[nn];
+                    if (g.relu) v = fmaxf(v, 0.f);
+                    g.C[(long long)m * g.ldc + nn] = v;
+                    if (g.Cbf) g.Cbf[(long long)m * g.ldc + nn] = __float2bfloat16(v);
+                }
+}
+
+cudaError_t gemm(const GemmArgs& g, cudaStream_t st)
+{
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
+    dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M);
+    k_gemm_bf16<<<grid, 128, 0, st>>>(g);
+    return cudaGetLastError();
+}
+
+// dY := dY * (Y > 0)  (ReLU backward, in place on the FP32 gradient)
+__global__ void k_relu_back(long long n, const float* __restrict__ y, float* __restrict__ dy)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        if (!(y[i] > 0.f)) dy[i] = 0.f;
+}
+
+// column sums: db[j] = sum_i dY[i][j]  (one thread per column, fixed order)
+__global__ void k_colsum(int M, int N, const float* __restrict__ dy, float* __restrict__ db)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= N) return;
+    float s = 0.f;
+    for (int i = 0; i < M; ++i) s += dy[(long long)i * N + j];
+    db[j] = s;
+}
+
+// mean-squared-error gradient: d = (pred - target) * 2 / (M * n_out); loss partial sums
+__global__ void k_mse(long long n, float scale, const float* __restrict__ pred, const float* __restrict__ tgt,
+                      float* __restrict__ d, double* __restrict__ loss)
+{
+    __shared__ double red[34];
+    double s = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float e = pred[i] - tgt[i];
+        d[i] = 2.f * scale * e;
+        s += (double)e * e;
+    }
+    s = block_sum(s, red);
+    if (threadIdx.x == 0) atomicAdd(loss, s * scale);
+}
+
+__global__ void k_adam(long long n, float lr, float b1, float b2, float eps, float c1, float c2,
+                       float* __restrict__ w, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, __nv_bfloat16* __restrict__ wbf)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float gi = g[i];
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float wi = w[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        w[i] = wi;
+        if (wbf) wbf[i] = __float2bfloat16(wi);
+    }
+}
+
+__global__ void k_to_bf16(long long n, const float* __restrict__ a, __nv_bfloat16* __restrict__ b)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        b[i] = __float2bfloat16(a[i]);
+}
+
+int g1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); }
+
+}  // namespace
+
+// ------------------------------------------------------------------ model
+struct sem_learner {
+    int d_in = 0, H = 0, d_out = 0;
+    // parameters: FP32 master, BF16 copies for the GEMMs, Adam moments, gradients
+    float *W[3] = {}, *b[3] = {}, *gW[3] = {}, *gb[3] = {}, *mW[3] = {}, *vW[3] = {}, *mb[3] = {}, *vb[3] = {};
+    __nv_bfloat16* Wbf[3] = {};
+    int rows_cap = 0;
+    float *h1 = nullptr, *h2 = nullptr, *out = nullptr, *d2 = nullptr, *d1 = nullptr, *dout = nullptr;
+    __nv_bfloat16 *h1bf = nullptr, *h2bf = nullptr;
+    double* loss = nullptr;
+    long long adam_t = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int din(int l) const { return l == 0 ? d_in : H; }
+    int dout_(int l) const { return l == 2 ? d_out : H; }
+};
+
+static int lfail(sem_learner* L, int code, const std::string& m)
+{
+    if (L) L->err = m;
+    return ctx_fail(code, m.c_str());
+}
+
+#define LCUDA(call)                                                                                  \
+    do {                                                                                             \
+        cudaError_t e_ = (call);                                                                     \
+        if (e_ != cudaSuccess) return lfail(L, SEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+static int ensure_rows(sem_learner* L, int rows)
+{
+    if (rows <= L->rows_cap) return SEM_OK;
+    float** fb[] = {&L->h1, &L->h2, &L->out, &L->d2, &L->d1, &L->dout};
+    for (float** p : fb)
+        if (*p) cudaFree(*p);
+    if (L->h1bf) cudaFree(L->h1bf);
+    if (L->h2bf) cudaFree(L->h2bf);
+    const size_t r = (size_t)rows;
+    LCUDA(cudaMalloc(&L->h1, r * L->H * 4));
+    LCUDA(cudaMalloc(&L->h2, r * L->H * 4));
+    LCUDA(cudaMalloc(&L->d1, r * L->H * 4));
+    LCUDA(cudaMalloc(&L->d2, r * L->H * 4));
+    LCUDA(cudaMalloc(&L->out, r * L->d_out * 4));
+    LCUDA(cudaMalloc(&L->dout, r * L->d_out * 4));
+    LCUDA(cudaMalloc(&L->h1bf, r * L->H * 2));
+    LCUDA(cudaMalloc(&L->h2bf, r * L->H * 2));
+    L->rows_cap = rows;
+    return SEM_OK;
+}
+
+extern "C" int sem_learner_create(sem_learner** out, int d_in, int hidden, int d_out, unsigned long long seed)
+{
+    if (!out || d_in <= 0 || hidden <= 0 || d_out <= 0) return ctx_fail(SEM_ERR_ARG, "bad learner shape");
+    sem_learner* L = new sem_learner();
+    L->d_in = d_in;
+    L->H = hidden;
+    L->d_out = d_out;
+    LCUDA(cudaMalloc(&L->loss, sizeof(double)));
+    // He-uniform initialisation from a splitmix64 stream (host), biases zero
+    uint64_t s = seed ? seed : 0x9E3779B97F4A7C15ull;
+    auto next = [&]() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        z ^= z >> 31;
+        return (double)(z >> 11) * (1.0 / 9007199254740992.0);
+    };
+    for (int l = 0; l < 3; ++l) {
+        const size_t nw = (size_t)L->din(l) * L->dout_(l), nb = (size_t)L->dout_(l);
+        std::vector<float> w(nw), z(nw > nb ? nw : nb, 0.f);
+        const double a = std::sqrt(6.0 / L->din(l)) * (l == 2 ? 0.1 : 1.0);
+        for (auto& v : w) v = (float)((2.0 * next() - 1.0) * a);
+        float** bufs[] = {&L->W[l], &L->gW[l], &L->mW[l], &L->vW[l]};
+        for (float** p : bufs) LCUDA(cudaMalloc(p, nw * 4));
+        float** bb[] = {&L->b[l], &L->gb[l], &L->mb[l], &L->vb[l]};
+        for (float** p : bb) LCUDA(cudaMalloc(p, nb * 4));
+        LCUDA(cudaMalloc(&L->Wbf[l], nw * 2));
+        LCUDA(cudaMemcpy(L->W[l], w.data(), nw * 4, cudaMemcpyHostToDevice));
+        LCUDA(cudaMemset(L->mW[l], 0, nw * 4));
+        LCUDA(cudaMemset(L->vW[l], 0, nw * 4));
+        LCUDA(cudaMemset(L->b[l], 0, nb * 4));
+        LCUDA(cudaMemset(L->mb[l], 0, nb * 4));
+        LCUDA(cudaMemset(L->vb[l], 0, nb * 4));
+        k_to_bf16<<<g1d(nw), 256>>>(nw, L->W[l], L->Wbf[l]);
+        LCUDA(cudaGetLastError());
+    }
+    LCUDA(cudaDeviceSynchronize());
+    *out = L;
+    return SEM_OK;
+}
+
+extern "C" int sem_learner_destroy(sem_learner* L)
+{
+    if (!L) return SEM_OK;
+    cudaDeviceSynchronize();
+    for (int l = 0; l < 3; ++l) {
+        float* f[] = {L->W[l], L->b[l], L->gW[l], L->gb[l], L->mW[l], L->vW[l], L->mb[l], L->vb[l]};
+        for (float* p : f)
+            if (p) cudaFree(p);
+        if (L->Wbf[l]) cudaFree(L->Wbf[l]);
+    }
+    float* f2[] = {L->h1, L->h2, L->out, L->d2, L->d1, L->dout};
+    for (float* p : f2)
+        if (p) cudaFree(p);
+    if (L->h1bf) cudaFree(L->h1bf);
+    if (L->h2bf) cudaFree(L->h2bf);
+    if (L->loss) cudaFree(L->loss);
+    delete L;
+    return SEM_OK;
+}
+
+extern "C" int sem_learner_shape(const sem_learner* L, int* d_in, int* hidden, int* d_out)
+{
+    if (!L) return ctx_fail(SEM_ERR_ARG, "null learner");
+    if (d_in) *d_in = L->d_in;
+    if (hidden) *hidden = L->H;
+    if (d_out) *d_out = L->d_out;
+    return SEM_OK;
+}
+
+extern "C" int sem_learner_set_stream(sem_learner* L, void* stream)
+{
+    if (!L) return ctx_fail(SEM_ERR_ARG, "null learner");
+    L->stream = (cudaStream_t)stream;
+    return SEM_OK;
+}
+
+// host copies of the FP32 parameters of layer l (W: d_in(l) x d_out(l) row-major, b: d_out(l))
+extern "C" int sem_learner_get_params(sem_learner* L, int l, float* W, float* b)
+{
+    if (!L || l < 0 || l > 2) return ctx_fail(SEM_ERR_ARG, "bad layer");
+    LCUDA(cudaStreamSynchronize(L->stream));
+    if (W) LCUDA(cudaMemcpy(W, L->W[l], (size_t)L->din(l) * L->dout_(l) * 4, cudaMemcpyDeviceToHost));
+    if (b) LCUDA(cudaMemcpy(b, L->b[l], (size_t)L->dout_(l) * 4, cudaMemcpyDeviceToHost));
+    return SEM_OK;
+}
+
+extern "C" int sem_learner_set_params(sem_learner* L, int l, const float* W, const float* b)
+{
+    if (!L || l < 0 || l > 2) return ctx_fail(SEM_ERR_ARG, "bad layer");
+    const size_t nw = (size_t)L->din(l) * L->dout_(l);
+    if (W) {
+        LCUDA(cudaMemcpy(L->W[l], W, nw * 4, cudaMemcpyHostToDevice));
+        k_to_bf16<<<g1d(nw), 256, 0, L->stream>>>(nw, L->W[l], L->Wbf[l]);
+        LCUDA(cudaGetLastError());
+    }
+    if (b) LCUDA(cudaMemcpy(L->b[l], b, (size_t)L->dout_(l) * 4, cudaMemcpyHostToDevice));
+    LCUDA(cudaStreamSynchronize(L->stream));
+    return SEM_OK;
+}
+
+// x: rows x d_in (device, BF16) -> L->out (FP32, rows x d_out)
+static int forward(sem_learner* L, int rows, const __nv_bfloat16* x)
+{
+    int s = ensure_rows(L, rows);
+    if (s) return s;
+    GemmArgs g{};
+    g.M = rows; g.N = L->H; g.K = L->d_in;
+    g.A = x; g.sa_m = L->d_in; g.sa_k = 1; g.a_bf16 = 1;
+    g.B = L->Wbf[0]; g.sb_k = L->H; g.sb_n = 1; g.b_bf16 = 1;
+    g.C = L->h1; g.ldc = L->H; g.bias = L->b[0]; g.relu = 1; g.Cbf = L->h1bf;
+    LCUDA(gemm(g, L->stream));
+    g.K = L->H; g.A = L->h1bf; g.sa_m = L->H;
+    g.B = L->Wbf[1]; g.C = L->h2; g.bias = L->b[1]; g.Cbf = L->h2bf;
+    LCUDA(gemm(g, L->stream));
+    g.N = L->d_out; g.A = L->h2bf; g.B = L->Wbf[2]; g.sb_k = L->d_out;
+    g.C = L->out; g.ldc = L->d_out; g.bias = L->b[2]; g.relu = 0; g.Cbf = nullptr;
+    LCUDA(gemm(g, L->stream));
+    return SEM_OK;
+}
+
+// predictions for rows x d_in BF16 inputs into out (device FP32, rows x d_out)
+extern "C" int sem_learner_forward(sem_learner* L, int rows, const void* x_bf16, float* out)
+{
+    if (!L || rows < 0 || !x_bf16 || !out) return ctx_fail(SEM_ERR_ARG, "bad forward arguments");
+    int s = forward(L, rows, (const __nv_bfloat16*)x_bf16);
+    if (s) return s;
+    LCUDA(cudaMemcpyAsync(out, L->out, (size_t)rows * L->d_out * 4, cudaMemcpyDeviceToDevice, L->stream));
+    return SEM_OK;
+}
+
+// gradients of the mean-squared error for one batch (device inputs); loss
+// (mean over rows and outputs) to *loss_out; with lr > 0 also one Adam step
+extern "C" int sem_learner_train_step(sem_learner* L, int rows, const void* x_bf16, const float* target,
+                                      float lr, double* loss_out)
+{
+    if (!L || rows <= 0 || !x_bf16 || !target) return ctx_fail(SEM_ERR_ARG, "bad train arguments");
+    const __nv_bfloat16* x = (const __nv_bfloat16*)x_bf16;
+    int s = forward(L, rows, x);
+    if (s) return s;
+    const long long no = (long long)rows * L->d_out;
+    LCUDA(cudaMemsetAsync(L->loss, 0, sizeof(double), L->stream));
+    k_mse<<<g1d(no), 256, 0, L->stream>>>(no, 1.f / (float)no, L->out, target, L->dout, L->loss);
+    LCUDA(cudaGetLastError());
+    // layer 3: gW3 = h2^T dout, gb3 = colsum(dout), d2 = dout W3^T (masked by ReLU)
+    GemmArgs g{};
+    g.M = L->H; g.N = L->d_out; g.K = rows;
+    g.A = L->h2bf; g.sa_m = 1; g.sa_k = L->H; g.a_bf16 = 1;
+    g.B = L->dout; g.sb_k = L->d_out; g.sb_n = 1; g.b_bf16 = 0;
+    g.C = L->gW[2]; g.ldc = L->d_out;
+    LCUDA(gemm(g, L->stream));
+    k_colsum<<<(L->d_out + 127) / 128, 128, 0, L->stream>>>(rows, L->d_out, L->dout, L->gb[2]);
+    g = GemmArgs{};
+    g.M = rows; g.N = L->H; g.K = L->d_out;
+    g.A = L->dout; g.sa_m = L->d_out; g.sa_k = 1; g.a_bf16 = 0;
+    g.B = L->Wbf[2]; g.sb_k = 1; g.sb_n = L->d_out; g.b_bf16 = 1;
+    g.C = L->d2; g.ldc = L->H;
+    LCUDA(gemm(g, L->stream));
+    k_relu_back<<<g1d((long long)rows * L->H), 256, 0, L->stream>>>((long long)rows * L->H, L->h2, L->d2);
+    // layer 2
+    g = GemmArgs{};
+    g.M = L->H; g.N = L->H; g.K = rows;
+    g.A = L->h1bf; g.sa_m = 1; g.sa_k = L->H; g.a_bf16 = 1;
+    g.B = L->d2; g.sb_k = L->H; g.sb_n = 1; g.b_bf16 = 0;
+    g.C = L->gW[1]; g.ldc = L->H;
+    LCUDA(gemm(g, L->stream));
+    k_colsum<<<(L->H + 127) / 128, 128, 0, L->stream>>>(rows, L->H, L->d2, L->gb[1]);
+    g = GemmArgs{};
+    g.M = rows; g.N = L->H; g.K = L->H;
+    g.A = L->d2; g.sa_m = L->H; g.sa_k = 1; g.a_bf16 = 0;
+    g.B = L->Wbf[1]; g.sb_k = 1; g.sb_n = L->H; g.b_bf16 = 1;
+    g.C = L->d1; g.ldc = L->H;
+    LCUDA(gemm(g, L->stream));
+    k_relu_back<<<g1d((long long)rows * L->H), 256, 0, L->stream>>>((long long)rows * L->H, L->h1, L->d1);
+    // layer 1
+    g = GemmArgs{};
+    g.M = L->d_in; g.N = L->H; g.K = rows;
+    g.A = x; g.sa_m = 1; g.sa_k = L->d_in; g.a_bf16 = 1;
+    g.B = L->d1; g.sb_k = L->H; g.sb_n = 1; g.b_bf16 = 0;
+    g.C = L->gW[0]; g.ldc = L->H;
+    LCUDA(gemm(g, L->stream));
+    k_colsum<<<(L->H + 127) / 128, 128, 0, L->stream>>>(rows, L->H, L->d1, L->gb[0]);
+    LCUDA(cudaGetLastError());
+    if (lr > 0.f) {
+        ++L->adam_t;
+        const float b1 = 0.9f, b2 = 0.999f;
+        const float c1 = 1.f - std::pow(b1, (float)L->adam_t), c2 = 1.f - std::pow(b2, (float)L->adam_t);
+        for (int l = 0; l < 3; ++l) {
+            const long long nw = (long long)L->din(l) * L->dout_(l), nb = L->dout_(l);
+            k_adam<<<g1d(nw), 256, 0, L->stream>>>(nw, lr, b1, b2, 1e-8f, c1, c2, L->W[l], L->gW[l], L->mW[l],
+                                                   L->vW[l], L->Wbf[l]);
+            k_adam<<<g1d(nb), 256, 0, L->stream>>>(nb, lr, b1, b2, 1e-8f, c1, c2, L->b[l], L->gb[l], L->mb[l],
+                                                   L->vb[l], nullptr);
+        }
+        LCUDA(cudaGetLastError());
+    }
+    if (loss_out) {
+        LCUDA(cudaMemcpyAsync(loss_out, L->loss, sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+        LCUDA(cudaStreamSynchronize(L->stream));
+    }
+    return SEM_OK;
+}
+
+// host copies of the last train step's gradients of layer l
+extern "C" int sem_learner_get_grads(sem_learner* L, int l, float* gW, float* gb)
+{
+    if (!L || l < 0 || l > 2) return ctx_fail(SEM_ERR_ARG, "bad layer");
+    LCUDA(cudaStreamSynchronize(L->stream));
+    if (gW) LCUDA(cudaMemcpy(gW, L->gW[l], (size_t)L->din(l) * L->dout_(l) * 4, cudaMemcpyDeviceToHost));
+    if (gb) LCUDA(cudaMemcpy(gb, L->gb[l], (size_t)L->dout_(l) * 4, cudaMemcpyDeviceToHost));
+    return SEM_OK;
+}
+
+namespace {
+__global__ void k_gather_rows(int rows, int dx, int dt, const int* __restrict__ idx,
+                              const __nv_bfloat16* __restrict__ X, const float* __restrict__ T,
+                              __nv_bfloat16* __restrict__ Xb, float* __restrict__ Tb)
+{
+    const long long total_x = (long long)rows * dx, total_t = (long long)rows * dt;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total_x; i += (long long)gridDim.x * blockDim.x)
+        Xb[i] = X[(long long)idx[i / dx] * dx + i % dx];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total_t; i += (long long)gridDim.x * blockDim.x)
+        Tb[i] = T[(long long)idx[i / dt] * dt + i % dt];
+}
+}  // namespace
+
+// Adam on the mean-squared error over a dataset of `rows` (BF16 inputs X,
+// FP32 targets T, device), in shuffled minibatches; mean loss of the last
+// epoch to *final_loss.
+extern "C" int sem_learner_fit(sem_learner* L, const void* X, const float* T, long long rows, int epochs,
+                               int batch, float lr, unsigned long long seed, double* final_loss)
+{
+    if (!L || !X || !T || rows <= 0 || epochs <= 0 || batch <= 0) return ctx_fail(SEM_ERR_ARG, "bad fit arguments");
+    const int dx = L->d_in, dt = L->d_out;
+    const int B = (int)std::min<long long>(batch, rows);
+    int* didx = nullptr;
+    __nv_bfloat16* Xb = nullptr;
+    float* Tb = nullptr;
+    LCUDA(cudaMalloc(&didx, sizeof(int) * B));
+    LCUDA(cudaMalloc(&Xb, sizeof(__nv_bfloat16) * (size_t)B * dx));
+    LCUDA(cudaMalloc(&Tb, sizeof(float) * (size_t)B * dt));
+    std::vector<int> perm((size_t)rows);
+    for (long long i = 0; i < rows; ++i) perm[(size_t)i] = (int)i;
+    uint64_t s = seed ? seed : 12345u;
+    auto next = [&]() {
+        s += 0x9E3779B97F4A7C15ull;
+        uint64_t z = s;
+        z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+        z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+        return z ^ (z >> 31);
+    };
+    double last = 0.0;
+    int status = SEM_OK;
+    for (int ep = 0; ep < epochs && status == SEM_OK; ++ep) {
+        for (long long i = rows - 1; i > 0; --i) std::swap(perm[(size_t)i], perm[(size_t)(next() % (uint64_t)(i + 1))]);
+        double sum = 0.0;
+        int nb = 0;
+        for (long long b0 = 0; b0 + B <= rows; b0 += B) {
+            cudaMemcpyAsync(didx, perm.data() + b0, sizeof(int) * B, cudaMemcpyHostToDevice, L->stream);
+            k_gather_rows<<<g1d((long long)B * dx), 256, 0, L->stream>>>(B, dx, dt, didx, (const __nv_bfloat16*)X, T,
+                                                                         Xb, Tb);
+            double loss = 0.0;
+            status = sem_learner_train_step(L, B, Xb, Tb, lr, &loss);
+            if (status) break;
+            sum += loss;
+            ++nb;
+        }
+        last = nb ? sum / nb : 0.0;
+    }
+    cudaFree(didx);
+    cudaFree(Xb);
+    cudaFree(Tb);
+    if (status) return status;
+    if (final_loss) *final_loss = last;
+    return SEM_OK;
+}
+
+// generic BF16 tensor-core GEMM exposed for testing: C(M x N, FP32, row-major)
+// = A(M x K, BF16 row-major) * B(K x N, BF16 row-major)
+extern "C" int sem_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, void* stream)
+{
+    if (M < 0 || N < 0 || K < 0 || (M && N && K && (!A || !B || !C))) return ctx_fail(SEM_ERR_ARG, "bad gemm");
+    GemmArgs g{};
+    g.M = M; g.N = N; g.K = K;
+    g.A = A; g.sa_m = K; g.sa_k = 1; g.a_bf16 = 1;
+    g.B = B; g.sb_k = N; g.sb_n = 1; g.b_bf16 = 1;
+    g.C = C; g.ldc = N;
+    cudaError_t e = gemm(g, (cudaStream_t)stream);
+    if (e != cudaSuccess) return ctx_fail(SEM_ERR_CUDA, cudaGetErrorString(e));
+    return SEM_OK;
+}

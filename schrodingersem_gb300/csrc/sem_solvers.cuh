@@ -3,6 +3,11 @@
 // SOLVER_TPB threads; each block owns a contiguous element range and stages
 // up to kmax of its elements per pass in dynamic shared memory
 // (apply_range).  Grid-wide phases are separated by bounded grid barriers.
+//
+// Scalar recurrences (Givens rotations, step lengths, stopping tests) run in
+// FP64 on one thread per block and are broadcast through shared memory, with
+// T-typed copies of the per-pass coefficients: GB300's FP64 pipe is 1/58 of
+// FP32, so redundant per-thread scalar FP64 code would dominate small passes.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -21,6 +26,133 @@ struct MinresOut {
     bool conv;
 };
 
+// block sum of per-thread T partials: warp shuffles in T, then FP64 across
+// warps (fixed order); result returned to every thread
+template <typename T>
+__device__ __forceinline__ double block_sum_t(T v, double* red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) red[wid] = (double)v;
+    __syncthreads();
+    if (wid == 0) {
+        const int nw = (blockDim.x + 31) >> 5;
+        double s = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) red[32] = s;
+    }
+    __syncthreads();
+    return red[32];
+}
+
+// grid all-reduce of up to two T partials (one barrier); see grid_sum2
+template <typename T>
+__device__ __forceinline__ void grid_sum2_t(T v0, T v1, double* partials, int slot, GridSync* gs, long long tmo,
+                                            double* red, bool& ok, double& r0, double& r1)
+{
+    const double b0 = block_sum_t<T>(v0, red);
+    const double b1 = block_sum_t<T>(v1, red);
+    const int G = gridDim.x;
+    double* p0 = partials + (size_t)(slot * 2) * G;
+    double* p1 = p0 + G;
+    if (threadIdx.x == 0) {
+        p0[blockIdx.x] = b0;
+        p1[blockIdx.x] = b1;
+    }
+    ok = grid_barrier(gs, tmo);
+    if (threadIdx.x < 32) {
+        double s0 = 0.0, s1 = 0.0;
+        for (int q = threadIdx.x; q < G; q += 32) {
+            s0 += __ldcg(p0 + q);
+            s1 += __ldcg(p1 + q);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            s0 += __shfl_xor_sync(0xffffffffu, s0, o);
+            s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+        }
+        if (threadIdx.x == 0) {
+            red[33] = s0;
+            red[32] = s1;
+        }
+    }
+    __syncthreads();
+    r0 = red[33];
+    r1 = red[32];
+    __syncthreads();
+}
+
+// MINRES scalar state (minres.hpp:28-40, 65-84), shared memory, thread 0 only
+template <typename T>
+struct MinresScal {
+    double bnorm, beta, beta_old, phibar, cs, sn, dbar, eps;
+    double pg, peps, pdelta, pphi, pinvb, alpha_i;
+    int pending, conv, stop;
+    // coefficients of the next vector pass, in T
+    T inv_b, c1, c2, cq, tpg, tpeps, tpdelta, tpphi, tpinvb;
+};
+
+template <typename T>
+__device__ __forceinline__ void scal_init(MinresScal<T>& sc, double bnorm, double beta1)
+{
+    sc.bnorm = bnorm;
+    sc.beta = beta1;
+    sc.beta_old = 0.0;
+    sc.phibar = beta1;
+    sc.cs = -1.0;
+    sc.sn = 0.0;
+    sc.dbar = 0.0;
+    sc.eps = 0.0;
+    sc.pg = sc.peps = sc.pdelta = sc.pphi = sc.pinvb = sc.alpha_i = 0.0;
+    sc.pending = 0;
+    sc.conv = 0;
+    sc.stop = 0;
+}
+
+// coefficients of pass `it` (Phase B / fused pass)
+template <typename T>
+__device__ __forceinline__ void scal_publish(MinresScal<T>& sc, int it, double cq)
+{
+    sc.inv_b = (T)(1.0 / sc.beta);
+    sc.c1 = (T)(it >= 2 ? sc.beta / sc.beta_old : 0.0);
+    sc.cq = (T)cq;
+    sc.tpg = (T)sc.pg;
+    sc.tpeps = (T)sc.peps;
+    sc.tpdelta = (T)sc.pdelta;
+    sc.tpphi = (T)sc.pphi;
+    sc.tpinvb = (T)sc.pinvb;
+}
+
+// Givens rotation of one iteration (minres.hpp:65-92)
+template <typename T>
+__device__ __forceinline__ void scal_givens(MinresScal<T>& sc, double alpha_i, double beta_new, double eps_mach,
+                                            double tol_rel, double tol_abs)
+{
+    const double eps_old = sc.eps;
+    const double delta = sc.cs * sc.dbar + sc.sn * alpha_i;
+    const double gbar = sc.sn * sc.dbar - sc.cs * alpha_i;
+    sc.eps = sc.sn * beta_new;
+    sc.dbar = -sc.cs * beta_new;
+    double gamma = sqrt(gbar * gbar + beta_new * beta_new);
+    if (gamma < eps_mach) gamma = eps_mach;
+    sc.cs = gbar / gamma;
+    sc.sn = beta_new / gamma;
+    const double phi = sc.cs * sc.phibar;
+    sc.phibar *= sc.sn;
+    sc.pending = 1;
+    sc.pg = 1.0 / gamma;
+    sc.peps = eps_old;
+    sc.pdelta = delta;
+    sc.pphi = phi;
+    sc.pinvb = 1.0 / sc.beta;
+    sc.beta_old = sc.beta;
+    sc.beta = beta_new;
+    sc.conv = sc.phibar < tol_rel * sc.bnorm + tol_abs;  // minres.hpp:92
+}
+
 // include/minres.hpp:19-107 inside a cooperative kernel.  Lanczos vectors
 // are kept in the continuous format (every copy of a shared node holds the
 // assembled value, boundary zero) so the operator needs no gather; dots
@@ -37,7 +169,7 @@ struct MinresOut {
 // rhs(ni, e, flat, c) gives the initial residual (continuous format) at a
 // node.  Returns false when a grid barrier timed out.
 template <int N, typename T, int OP, bool PRE, class Rhs>
-__device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const DevMesh& m,
+__device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, MinresScal<T>& sc, const DevMesh& m,
                                             const T* pot, T alpha, int eb, int ee,
                                             const KrylovWork<T>& w, GridSync* gs, long long tmo,
                                             int& slot, Rhs&& rhs, T* const* xp, int maxit,
@@ -49,6 +181,7 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
     const Fac<T> fac = fac_of<T>(m);
     const long long n = m.n;
     const long long nb = (long long)eb * NN, ne = (long long)ee * NN;
+    const double eps_mach = (double)std::numeric_limits<T>::epsilon();
     bool ok = true;
     T* L[3] = {w.L[0], w.L[1], w.L[2]};
     T* W[3] = {w.W[0], w.W[1], w.W[2]};
@@ -61,7 +194,7 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
         };
     };
     // P1: r; |r|^2 and r.z (z = P^-1 r); W[0] = W[1] = 0; Y[0] = A_local(z)
-    double part = 0.0, partz = 0.0;
+    T part = T(0), partz = T(0);
     for (int e0 = eb; e0 < ee; e0 += kmax)
         apply_range<N, T, OP>(
             sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
@@ -78,36 +211,30 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
                     const T z = PRE ? pv * r : r;
                     u[c] = z;
                     if (own) {
-                        part = fma((double)r, (double)r, part);
-                        if (PRE) partz = fma((double)r, (double)z, partz);
+                        part = fma(r, r, part);
+                        partz = fma(r, z, partz);
                     }
                 }
             },
             store_y(w.Y[0]));
-    const double bb = grid_sum(part, w.partials, slot, gs, tmo, red, ok);
+    double bb = 0.0, bz = 0.0;
+    grid_sum2_t<T>(part, partz, w.partials, slot, gs, tmo, red, ok, bb, bz);
     slot ^= 1;
     if (!ok) return false;
-    double bz = bb;
-    if (PRE) {
-        bz = grid_sum(partz, w.partials, slot, gs, tmo, red, ok);
-        slot ^= 1;
-        if (!ok) return false;
+    if (threadIdx.x == 0) {
+        scal_init(sc, sqrt(bb), sqrt(bz));  // minres.hpp:28,31
+        scal_publish(sc, 1, 0.0);
     }
-
-    const double eps_mach = (double)std::numeric_limits<T>::epsilon();
-    const double bnorm = sqrt(bb);  // minres.hpp:28 (Euclidean, for the stopping test)
-    const double beta1 = sqrt(bz);  // minres.hpp:31, sqrt(y.r1) with y = P^-1 r1
-    double beta = beta1, beta_old = 0.0, phibar = beta1, cs = -1.0, sn = 0.0, dbar = 0.0, eps = 0.0;
-    double pg = 0.0, peps = 0.0, pdelta = 0.0, pphi = 0.0, pinvb = 0.0;
-    bool pending = false, conv = false;
+    __syncthreads();
     int it = 1;
     if (maxit >= 1) {
         for (;;) {
             // ---- Phase B_it
-            const T inv_b = (T)(1.0 / beta);
-            const T c1 = (T)(it >= 2 ? beta / beta_old : 0.0);
+            const T inv_b = sc.inv_b, c1 = sc.c1;
+            const bool pending = sc.pending != 0;
+            const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
             const T* Ycur = w.Y[(it - 1) & 1];
-            double s1 = 0.0;
+            T s1 = T(0);
 #pragma unroll 4
             for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
                 const int e = (int)(idx / NN);
@@ -126,13 +253,13 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
                         y3 = av - c1 * r1v;
                     }
                     const T vv = inv_b * (PRE ? pv * L[ir2][q] : L[ir2][q]);
-                    if (own) s1 = fma((double)vv, (double)y3, s1);
+                    if (own) s1 = fma(vv, y3, s1);
                     L[iy][q] = y3;
                     if (pending) {
-                        const T vprev = (T)pinvb * (PRE ? pv * r1v : r1v);
-                        const T wn = (T)pg * ((vprev - (T)peps * W[iw1][q]) - (T)pdelta * W[iw2][q]);
+                        const T vprev = tpinvb * (PRE ? pv * r1v : r1v);
+                        const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
                         W[iw][q] = wn;
-                        if (own) xp[c][idx] += (T)pphi * wn;
+                        if (own) xp[c][idx] += tpphi * wn;
                     }
                 }
             }
@@ -141,14 +268,20 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
                 iw1 = iw2;
                 iw2 = iw;
                 iw = tmp;
-                pending = false;
             }
-            const double alpha_i = grid_sum(s1, w.partials, slot, gs, tmo, red, ok);
+            double S1 = 0.0, dummy = 0.0;
+            grid_sum2_t<T>(s1, T(0), w.partials, slot, gs, tmo, red, ok, S1, dummy);
             slot ^= 1;
             if (!ok) return false;
+            if (threadIdx.x == 0) {
+                sc.pending = 0;
+                sc.alpha_i = S1;
+                sc.c2 = (T)(S1 / sc.beta);
+            }
+            __syncthreads();
             // ---- Phase A_it+1
-            const T c2 = (T)(alpha_i / beta);
-            double ss = 0.0;
+            const T c2 = sc.c2;
+            T ss = T(0);
             T* Ynext = w.Y[it & 1];
             for (int e0 = eb; e0 < ee; e0 += kmax)
                 apply_range<N, T, OP>(
@@ -163,45 +296,31 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
                             L[iy][q] = y5;
                             const T z = PRE ? pv * y5 : y5;  // y = precond(r2), minres.hpp:60
                             u[c] = z;
-                            if (own) ss = fma((double)y5, (double)z, ss);
+                            if (own) ss = fma(y5, z, ss);
                         }
                     },
                     store_y(Ynext));
-            const double bnew2 = grid_sum(ss, w.partials, slot, gs, tmo, red, ok);
+            double bnew2 = 0.0;
+            grid_sum2_t<T>(ss, T(0), w.partials, slot, gs, tmo, red, ok, bnew2, dummy);
             slot ^= 1;
             if (!ok) return false;
-            const double beta_new = sqrt(bnew2);
             {
                 const int tmp = ir1;
                 ir1 = ir2;
                 ir2 = iy;
                 iy = tmp;
             }
-            // ---- Givens rotation of iteration it (minres.hpp:65-84)
-            const double eps_old = eps;
-            const double delta = cs * dbar + sn * alpha_i;
-            const double gbar = sn * dbar - cs * alpha_i;
-            eps = sn * beta_new;
-            dbar = -cs * beta_new;
-            double gamma = sqrt(gbar * gbar + beta_new * beta_new);
-            if (gamma < eps_mach) gamma = eps_mach;
-            cs = gbar / gamma;
-            sn = beta_new / gamma;
-            const double phi = cs * phibar;
-            phibar *= sn;
-            pending = true;
-            pg = 1.0 / gamma;
-            peps = eps_old;
-            pdelta = delta;
-            pphi = phi;
-            pinvb = 1.0 / beta;
-            beta_old = beta;
-            beta = beta_new;
-            conv = phibar < tol_rel * bnorm + tol_abs;  // minres.hpp:92
-            if (conv || it == maxit) break;
+            if (threadIdx.x == 0) {
+                scal_givens(sc, sc.alpha_i, sqrt(bnew2), eps_mach, tol_rel, tol_abs);
+                sc.stop = sc.conv || it == maxit;
+                scal_publish(sc, it + 1, 0.0);
+            }
+            __syncthreads();
+            if (sc.stop) break;
             ++it;
         }
         // ---- Phase F: w/x update of the last iteration
+        const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
         for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
             const int e = (int)(idx / NN);
             const int node = (int)(idx - (long long)e * NN);
@@ -211,15 +330,192 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, const 
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const long long q = c * n + idx;
-                const T vprev = (T)pinvb * (PRE ? pv * L[ir1][q] : L[ir1][q]);
-                const T wn = (T)pg * ((vprev - (T)peps * W[iw1][q]) - (T)pdelta * W[iw2][q]);
-                xp[c][idx] += (T)pphi * wn;
+                const T vprev = tpinvb * (PRE ? pv * L[ir1][q] : L[ir1][q]);
+                const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
+                xp[c][idx] += tpphi * wn;
             }
         }
     }
     res.it = it;
-    res.phibar = phibar;
-    res.conv = conv;
+    res.phibar = sc.phibar;
+    res.conv = sc.conv != 0;
+    __syncthreads();
+    return true;
+}
+
+// Single-barrier variant of minres_core (same recurrences, Givens rotations
+// and stopping test) for the Res operator in the FP32 inner solve.  The
+// element operator is linear, so the next operator product is carried as
+//   A z_{i+1} = DSS(A_local(P^-1 y_i)) - (alpha_i/beta_i) A z_i,
+// with A_local(P^-1 y_i) computed in the same pass that forms y_i, and
+//   beta_{i+1}^2 = y_i . P^-1 y_i - alpha_i^2
+// comes out of the same reduction as alpha_i = z_i . y_i / beta_i.  The
+// subtraction is benign for Res = [M, aL; aL, -M], whose spectrum is
+// symmetric about zero (Lanczos alpha_i stay small against beta_i); it
+// would cancel for one-sided spectra, which therefore use minres_core.
+// Rounding in the recurred A z is not re-anchored: the FP64 refinement
+// around the inner solve judges the true residual.
+template <int N, typename T, int OP, bool PRE, class Rhs>
+__device__ __forceinline__ bool minres_core_fused(T* sm, int kmax, double* red, MinresScal<T>& sc,
+                                                  const DevMesh& m, const T* pot, T alpha, int eb, int ee,
+                                                  const KrylovWork<T>& w, GridSync* gs, long long tmo,
+                                                  int& slot, Rhs&& rhs, T* const* xp, int maxit,
+                                                  double tol_rel, double tol_abs, MinresOut& res,
+                                                  const T* __restrict__ pinv)
+{
+    constexpr int NN = N * N;
+    constexpr int NC = op_nc<OP>();
+    const Fac<T> fac = fac_of<T>(m);
+    const long long n = m.n;
+    const long long nb = (long long)eb * NN, ne = (long long)ee * NN;
+    const double eps_mach = (double)std::numeric_limits<T>::epsilon();
+    bool ok = true;
+    T* Q[3] = {w.L[0], w.L[1], w.L[2]};  // q_i (= r2), q_{i-1} (= r1), free
+    T* W[3] = {w.W[0], w.W[1], w.W[2]};
+    T* TT[2] = {w.Y[0], w.Y[1]};         // element-local A_local(P^-1 y) ping-pong
+    T* AZ = w.AZ;
+    T* Y3 = w.Y3;
+    int iq = 0, iq1 = 1, iqf = 2;
+    int iw1 = 0, iw2 = 1, iw = 2;
+    auto store_t = [&](T* Tb) {
+        return [=](int, int, int, long long flat, const T* o) {
+#pragma unroll
+            for (int c = 0; c < NC; ++c) Tb[c * n + flat] = o[c];
+        };
+    };
+    // P1: q_1 = r0, z_1 = P^-1 q_1; |r0|^2, q_1.z_1; W[0] = W[1] = 0; T[1] = A_local(z_1)
+    T part = T(0), partz = T(0);
+    for (int e0 = eb; e0 < ee; e0 += kmax)
+        apply_range<N, T, OP>(
+            sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+            [&](int e, int i, int j, long long flat, T* u) {
+                const NodeInfo ni = node_info<N>(m, e, i, j);
+                const bool own = ni_owner(ni);
+                const T pv = PRE ? pinv[flat] : T(1);
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const T r = rhs(ni, e, flat, c);
+                    Q[iq][c * n + flat] = r;
+                    W[iw1][c * n + flat] = T(0);
+                    W[iw2][c * n + flat] = T(0);
+                    const T z = PRE ? pv * r : r;
+                    u[c] = z;
+                    if (own) {
+                        part = fma(r, r, part);
+                        partz = fma(r, z, partz);
+                    }
+                }
+            },
+            store_t(TT[1]));
+    double bb = 0.0, bz = 0.0;
+    grid_sum2_t<T>(part, partz, w.partials, slot, gs, tmo, red, ok, bb, bz);
+    slot ^= 1;
+    if (!ok) return false;
+    if (threadIdx.x == 0) {
+        scal_init(sc, sqrt(bb), sqrt(bz));
+        scal_publish(sc, 1, 0.0);
+    }
+    __syncthreads();
+    int it = 1;
+    if (maxit >= 1) {
+        for (;;) {
+            const T inv_b = sc.inv_b, c1 = sc.c1, cq = sc.cq;
+            const bool pending = sc.pending != 0;
+            const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
+            const bool first = (it == 1);
+            const T* Tin = TT[it & 1];  // A_local of the previous pass
+            T* Tout = TT[(it + 1) & 1];
+            T s1 = T(0), s2 = T(0);
+            for (int e0 = eb; e0 < ee; e0 += kmax)
+                apply_range<N, T, OP>(
+                    sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+                    [&](int e, int i, int j, long long flat, T* u) {
+                        const NodeInfo ni = node_info<N>(m, e, i, j);
+                        const bool own = ni_owner(ni);
+                        const T pv = PRE ? pinv[flat] : T(1);
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) {
+                            const long long q = c * n + flat;
+                            const T tsum = dss_value<N, T, DSS_CONT>(m, Tin + c * n, ni, e, flat);
+                            T qi, az, r1v = T(0);
+                            if (first) {
+                                qi = Q[iq][q];
+                                az = tsum;
+                            } else {
+                                r1v = Q[iq1][q];
+                                qi = Y3[q] - cq * r1v;  // q_i = y_{i-1} - (alpha/beta) q_{i-1}
+                                az = tsum - cq * AZ[q];
+                                Q[iq][q] = qi;
+                            }
+                            AZ[q] = az;
+                            const T y = az * inv_b - c1 * r1v;
+                            Y3[q] = y;
+                            const T zi = PRE ? pv * qi : qi;
+                            const T py = PRE ? pv * y : y;
+                            if (own) {
+                                s1 = fma(zi, y, s1);
+                                s2 = fma(y, py, s2);
+                            }
+                            if (pending) {
+                                const T vprev = tpinvb * (PRE ? pv * r1v : r1v);
+                                const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
+                                W[iw][q] = wn;
+                                if (own) xp[c][flat] += tpphi * wn;
+                            }
+                            u[c] = py;
+                        }
+                    },
+                    store_t(Tout));
+            if (pending) {
+                const int tmp = iw1;
+                iw1 = iw2;
+                iw2 = iw;
+                iw = tmp;
+            }
+            double S1 = 0.0, S2 = 0.0;
+            grid_sum2_t<T>(s1, s2, w.partials, slot, gs, tmo, red, ok, S1, S2);
+            slot ^= 1;
+            if (!ok) return false;
+            {
+                const int tmp = iqf;  // the next pass writes q_{i+1} into the free slot
+                iqf = iq1;
+                iq1 = iq;
+                iq = tmp;
+            }
+            if (threadIdx.x == 0) {
+                const double alpha_i = S1 / sc.beta;
+                double bnew2 = S2 - alpha_i * alpha_i;
+                if (bnew2 < 0.0) bnew2 = 0.0;
+                const double cnext = alpha_i / sc.beta;
+                scal_givens(sc, alpha_i, sqrt(bnew2), eps_mach, tol_rel, tol_abs);
+                sc.stop = sc.conv || it == maxit || sc.beta == 0.0;
+                scal_publish(sc, it + 1, cnext);
+            }
+            __syncthreads();
+            if (sc.stop) break;
+            ++it;
+        }
+        // ---- final w/x update of the last iteration (v = P^-1 q_it / beta_it; q_it is Q[iq1])
+        const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
+        for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
+            const int e = (int)(idx / NN);
+            const int node = (int)(idx - (long long)e * NN);
+            const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+            if (!ni_owner(ni)) continue;
+            const T pv = PRE ? pinv[idx] : T(1);
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                const long long q = c * n + idx;
+                const T vprev = tpinvb * (PRE ? pv * Q[iq1][q] : Q[iq1][q]);
+                const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
+                xp[c][idx] += tpphi * wn;
+            }
+        }
+    }
+    res.it = it;
+    res.phibar = sc.phibar;
+    res.conv = sc.conv != 0;
+    __syncthreads();
     return true;
 }
 
@@ -238,6 +534,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     constexpr int NC = op_nc<OP>();
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[34];
+    __shared__ MinresScal<T> sc;
     T* sm = (T*)smraw;
     load_dmat_raw<N, T>(sm, m);
     __syncthreads();
@@ -277,8 +574,8 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         return r;
     };
     MinresOut r{};
-    if (!minres_core<N, T, OP, false>(sm, kmax, red, m, pot, alpha, eb, ee, w, a.sync, a.timeout_ns,
-                                      slot, rhs, xp, a.maxit, a.tol, a.tol, r, (const T*)nullptr))
+    if (!minres_core<N, T, OP, false>(sm, kmax, red, sc, m, pot, alpha, eb, ee, w, a.sync, a.timeout_ns, slot,
+                                      rhs, xp, a.maxit, a.tol, a.tol, r, (const T*)nullptr))
         return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->success = r.conv ? 1 : 0;
@@ -292,9 +589,9 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
 // FP64 iterative refinement around an FP32 inner MINRES.  Each sweep:
 // r = b - A x in FP64 (true residual, continuous format); stop when
 // |r| < tol |r_0| + tol (for x_0 = 0 the reference's criterion minres.hpp:92
-// with the true residual in place of the recursive estimate); else solve
-// A d = r in FP32 to relative tolerance inner_tol and add d to x in FP64 on
-// owner copies.
+// with the true residual in place of the recursive estimate; with rel_to_b,
+// |b| replaces |r_0|); else solve A d = r in FP32 to relative tolerance
+// inner_tol and add d to x in FP64 on owner copies.
 template <int N, int OP>
 __global__ void __launch_bounds__(SOLVER_TPB, 1)
     k_minres_mixed(DevMesh m, SolveArgs a, KrylovWork<float> w, MixedArgs mx)
@@ -303,6 +600,8 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     constexpr int NC = op_nc<OP>();
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[34];
+    __shared__ MinresScal<float> sc;
+    __shared__ double sweep_state[3];  // r0, |r|, done
     double* sm64 = (double*)smraw;
     float* sm32 = (float*)smraw;
     const Fac<double> fac64 = fac_of<double>(m);
@@ -315,9 +614,8 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     const int kmax = a.kmax;
     int slot = 0;
     bool ok = true;
-    double r0 = 0.0, rn = 0.0;
-    bool conv = false;
     int sweep = 0, inner_total = 0;
+    bool conv = false;
     for (;;) {
         // ---- FP64 residual r = unmask(b) - DSS(A_local(unmask(x)))
         const bool applied = (sweep > 0) || !a.x_is_zero;
@@ -338,7 +636,8 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
                     });
             if (!grid_barrier(a.sync, a.timeout_ns)) return;
         }
-        double part = 0.0;
+        double part = 0.0, partb = 0.0;
+        const bool want_b = (sweep == 0) && a.rel_to_b;
 #pragma unroll 4
         for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
             const int e = (int)(idx / NN);
@@ -348,19 +647,34 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
             const bool own = ni_owner(ni);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
-                double r = bp[c][src];
+                const double bv = bp[c][src];
+                double r = bv;
                 if (applied) r = r - dss_value<N, double, DSS_CONT>(m, mx.Y64[c], ni, e, idx);
                 mx.r64[c][idx] = r;
                 mx.x32[c][idx] = 0.0f;
-                if (own) part = fma(r, r, part);
+                if (own) {
+                    part = fma(r, r, part);
+                    if (want_b) partb = fma(bv, bv, partb);
+                }
             }
         }
-        rn = sqrt(grid_sum(part, w.partials, slot, a.sync, a.timeout_ns, red, ok));
+        double rr = 0.0, bbv = 0.0;
+        grid_sum2_t<double>(part, partb, w.partials, slot, a.sync, a.timeout_ns, red, ok, rr, bbv);
         slot ^= 1;
         if (!ok) return;
-        if (sweep == 0) r0 = rn;
-        conv = rn < a.tol * r0 + a.tol;
-        if (conv || sweep >= mx.max_sweeps || inner_total >= a.maxit) break;
+        if (threadIdx.x == 0) {
+            const double rn = sqrt(rr);
+            if (sweep == 0) sweep_state[0] = want_b ? sqrt(bbv) : rn;
+            sweep_state[1] = rn;
+            const double r0 = sweep_state[0];
+            const bool c = rn < mx.outer_scale * (a.tol * r0 + a.tol);
+            sweep_state[2] = (c || sweep >= mx.max_sweeps || inner_total >= a.maxit) ? (c ? 2.0 : 1.0) : 0.0;
+        }
+        __syncthreads();
+        if (sweep_state[2] != 0.0) {
+            conv = sweep_state[2] == 2.0;
+            break;
+        }
         // ---- FP32 inner solve A d = r (relative tolerance inner_tol)
         load_dmat_raw<N, float>(sm32, m);
         __syncthreads();
@@ -368,13 +682,23 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         auto rhs = [&](const NodeInfo&, int, long long flat, int c) -> float { return (float)r64c[c][flat]; };
         MinresOut ir{};
         const int budget = min(mx.inner_maxit, a.maxit - inner_total);
-        const bool okc = mx.pinv32
-                             ? minres_core<N, float, OP, true>(sm32, kmax, red, m, mx.pot32, (float)a.alpha, eb, ee,
-                                                               w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
-                                                               mx.inner_tol, 0.0, ir, mx.pinv32)
-                             : minres_core<N, float, OP, false>(sm32, kmax, red, m, mx.pot32, (float)a.alpha, eb,
-                                                                ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
-                                                                budget, mx.inner_tol, 0.0, ir, (const float*)nullptr);
+        bool okc;
+        if (OP == OP_RES && mx.fused)
+            okc = mx.pinv32
+                      ? minres_core_fused<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb,
+                                                              ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
+                                                              budget, mx.inner_tol, 0.0, ir, mx.pinv32)
+                      : minres_core_fused<N, float, OP, false>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha,
+                                                               eb, ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
+                                                               budget, mx.inner_tol, 0.0, ir, (const float*)nullptr);
+        else
+            okc = mx.pinv32
+                      ? minres_core<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
+                                                        w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
+                                                        mx.inner_tol, 0.0, ir, mx.pinv32)
+                      : minres_core<N, float, OP, false>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
+                                                         w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
+                                                         mx.inner_tol, 0.0, ir, (const float*)nullptr);
         if (!okc) return;
         inner_total += ir.it;
         ++sweep;
@@ -388,7 +712,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->success = conv ? 1 : 0;
         a.out->n_iter = inner_total;
-        a.out->residual = rn;
+        a.out->residual = sweep_state[1];
         a.out->status = 0;
         a.out->inner_iters = inner_total;
         a.out->sweeps = sweep;
@@ -405,6 +729,8 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     constexpr int NN = N * N;
     extern __shared__ __align__(16) unsigned char smraw[];
     __shared__ double red[34];
+    __shared__ double ps[4];  // rho, rho_prev, bnorm, stop flag
+    __shared__ T pc[2];       // beta, alpha of the current iteration
     T* sm = (T*)smraw;
     load_dmat_raw<N, T>(sm, m);
     __syncthreads();
@@ -432,7 +758,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
                 store_y(w.Y[1]));
         if (!grid_barrier(a.sync, a.timeout_ns)) return;
     }
-    double pb = 0.0, pr = 0.0;
+    T pb = T(0), pr = T(0);
     for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
         const int e = (int)(idx / NN);
         const int node = (int)(idx - (long long)e * NN);
@@ -442,22 +768,27 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         if (!a.x_is_zero) r = bv - dss_value<N, T, DSS_CONT>(m, w.Y[1], ni, e, idx);
         R[idx] = r;
         if (ni_owner(ni)) {
-            pb = fma((double)bv, (double)bv, pb);
-            pr = fma((double)r, (double)r, pr);
+            pb = fma(bv, bv, pb);
+            pr = fma(r, r, pr);
         }
     }
-    const double bb = grid_sum(pb, w.partials, slot, a.sync, a.timeout_ns, red, ok);
+    double bb = 0.0, rho0 = 0.0;
+    grid_sum2_t<T>(pb, pr, w.partials, slot, a.sync, a.timeout_ns, red, ok, bb, rho0);
     slot ^= 1;
     if (!ok) return;
-    double rho = grid_sum(pr, w.partials, slot, a.sync, a.timeout_ns, red, ok);
-    slot ^= 1;
-    if (!ok) return;
-    const double bnorm = sqrt(bb);
-    double rho_prev = 0.0;
+    if (threadIdx.x == 0) {
+        ps[0] = rho0;
+        ps[1] = 0.0;
+        ps[2] = sqrt(bb);
+        ps[3] = 0.0;
+        pc[0] = T(0);
+    }
+    __syncthreads();
     bool conv = false;
     int it = 0;
+    double dummy = 0.0;
     for (it = 0; it < a.maxit; ++it) {
-        const T beta = (T)(it == 0 ? 0.0 : rho / rho_prev);
+        const T beta = pc[0];
         for (int e0 = eb; e0 < ee; e0 += kmax)
             apply_range<N, T, OP_LAPLACE>(
                 sm, kmax, fac, (const T*)nullptr, T(0), e0, min(kmax, ee - e0),
@@ -469,20 +800,22 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
                 store_y(w.Y[0]));
         // the assembly below reads other blocks' element outputs
         if (!grid_barrier(a.sync, a.timeout_ns)) return;
-        double pap = 0.0;
+        T pap = T(0);
 #pragma unroll 4
         for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
             const int e = (int)(idx / NN);
             const int node = (int)(idx - (long long)e * NN);
             const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
-            if (ni_owner(ni))
-                pap = fma((double)Pv[idx], (double)dss_value<N, T, DSS_CONT>(m, w.Y[0], ni, e, idx), pap);
+            if (ni_owner(ni)) pap = fma(Pv[idx], dss_value<N, T, DSS_CONT>(m, w.Y[0], ni, e, idx), pap);
         }
-        const double pAp = grid_sum(pap, w.partials, slot, a.sync, a.timeout_ns, red, ok);
+        double pAp = 0.0;
+        grid_sum2_t<T>(pap, T(0), w.partials, slot, a.sync, a.timeout_ns, red, ok, pAp, dummy);
         slot ^= 1;
         if (!ok) return;
-        const T al = (T)(rho / pAp);
-        double prr = 0.0;
+        if (threadIdx.x == 0) pc[1] = (T)(ps[0] / pAp);
+        __syncthreads();
+        const T al = pc[1];
+        T prr = T(0);
 #pragma unroll 4
         for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
             const int e = (int)(idx / NN);
@@ -493,19 +826,29 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
             if (own) x[idx] += al * Pv[idx];
             const T r = R[idx] - al * ap;
             R[idx] = r;
-            if (own) prr = fma((double)r, (double)r, prr);
+            if (own) prr = fma(r, r, prr);
         }
-        rho_prev = rho;
-        conv = sqrt(rho) < a.tol * bnorm;  // pcg.hpp:84, rho of this iteration's start
+        if (threadIdx.x == 0) {
+            ps[1] = ps[0];  // rho_prev = rho
+            ps[3] = sqrt(ps[0]) < a.tol * ps[2] ? 1.0 : 0.0;  // pcg.hpp:84, rho of this iteration's start
+        }
+        __syncthreads();
+        conv = ps[3] != 0.0;
         if (conv) break;
-        rho = grid_sum(prr, w.partials, slot, a.sync, a.timeout_ns, red, ok);
+        double rho = 0.0;
+        grid_sum2_t<T>(prr, T(0), w.partials, slot, a.sync, a.timeout_ns, red, ok, rho, dummy);
         slot ^= 1;
         if (!ok) return;
+        if (threadIdx.x == 0) {
+            pc[0] = (T)(rho / ps[1]);
+            ps[0] = rho;
+        }
+        __syncthreads();
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.out->success = conv ? 1 : 0;
         a.out->n_iter = it;
-        a.out->residual = sqrt(rho_prev);  // rho of the last iteration's start (pcg.hpp:93)
+        a.out->residual = sqrt(ps[1]);  // rho of the last iteration's start (pcg.hpp:93)
         a.out->status = 0;
     }
 }

@@ -108,3 +108,49 @@ def test_mixed_helmholtz(semlib, oracle, known):
     um = np.zeros(om.shape)
     assert ctx.helmholtz(um, c, f, 10 * om.dof(), 1e-10)[0]
     assert rel_err(om.unmask(um), om.unmask(u64)) < 1e-7
+
+
+def test_single_barrier_inner_iteration_matches_two_barrier(semlib, oracle):
+    from schrodingersem_gb300 import capi
+    ctx, om, re, im, V = _packet_case(semlib, oracle, n=10, p=8)
+    dV = ctx.to_device(V)
+    br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))
+    br.mul_(0.005)
+    bi.mul_(0.005)
+    alpha, tol = 0.005 * 1.0886, 1e-10
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    sols = {}
+    for mode in (0, 1):
+        ctx.set_option(capi.OPT_INNER_ITERATION, mode)
+        xr, xi = ctx.zeros(), ctx.zeros()
+        ok, it, res = ctx.minres_schro(dV, alpha, xr, xi, br, bi, 20 * ctx.dof(), tol, x_is_zero=True)
+        assert ok
+        sols[mode] = (it, xr.cpu().numpy(), xi.cpu().numpy())
+    # same recurrences up to rounding: iteration totals close, solutions equal to the tolerance
+    assert abs(sols[0][0] - sols[1][0]) <= max(10, sols[0][0] // 20)
+    for k in (1, 2):
+        assert rel_err(om.unmask(sols[1][k]), om.unmask(sols[0][k])) < 1e-7
+
+
+def test_extrapolated_stage_guess(semlib, oracle):
+    """the extrapolated guess changes only the iteration count: states agree
+    with the zero-guess FP64 run to 1e-8, and later steps need fewer
+    iterations.  The history carries over between single-step driver calls."""
+    from schrodingersem_gb300 import capi
+    ctx, om, re, im, V = _packet_case(semlib, oracle, n=8, p=6)
+    dt, tol, steps = 0.01, 1e-10, 6
+    a_re, a_im = re.copy(), im.copy()
+    assert ctx.schrodinger("dirk4s3", a_re, a_im, V, (steps - 0.5) * dt, dt, 20 * ctx.dof(), tol)
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    its = {}
+    for guess in (capi.GUESS_ZERO, capi.GUESS_EXTRAPOLATE):
+        ctx.set_option(capi.OPT_STAGE_GUESS, guess)
+        b_re, b_im = re.copy(), im.copy()
+        tot = []
+        for _ in range(steps):  # one driver call per step
+            assert ctx.schrodinger("dirk4s3", b_re, b_im, V, 0.5 * dt, dt, 20 * ctx.dof(), tol)
+            st = ctx.stats()
+            tot.append(sum(st.last_stage_iters[k] for k in range(st.last_step_stages)))
+        its[guess] = tot
+        assert max(rel_err(b_re, a_re), rel_err(b_im, a_im)) < 1e-8
+    assert sum(its[capi.GUESS_EXTRAPOLATE][2:]) < 0.9 * sum(its[capi.GUESS_ZERO][2:])
