@@ -63,9 +63,12 @@ enum sem_option {
     SEM_OPT_MAX_REFINE = 5,      /* cap on FP64 refinement sweeps in mixed mode (default 50) */
     SEM_OPT_PROFILE = 6,         /* 1: time every persistent solver launch with CUDA events */
     SEM_OPT_PRECOND = 7,         /* preconditioner of the FP32 inner solve in mixed mode:
-                                    SEM_PRECOND_NONE (default, as the reference) or
-                                    SEM_PRECOND_DIAG (diagonal of |A|); the FP64 outer test
-                                    on the true residual is unchanged */
+                                    SEM_PRECOND_NONE (default, as the reference),
+                                    SEM_PRECOND_DIAG (diagonal of |A|) or SEM_PRECOND_FDM
+                                    (Schroedinger Res only: per-element |A_e|^-1 by fast
+                                    diagonalisation of the element's rectangle approximation,
+                                    summed over elements with 1/multiplicity weights); the
+                                    FP64 outer test on the true residual is unchanged */
     SEM_OPT_INNER_ITERATION = 8, /* FP32 inner MINRES iteration for Res: 1 (default) one grid
                                     barrier per iteration (operator product carried by
                                     recurrence), 0 the two-barrier form of the FP64 solver */
@@ -73,7 +76,7 @@ enum sem_option {
                                     default 1 (the reference's test on the true residual) */
 };
 enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
-enum { SEM_PRECOND_NONE = 0, SEM_PRECOND_DIAG = 1 };
+enum { SEM_PRECOND_NONE = 0, SEM_PRECOND_DIAG = 1, SEM_PRECOND_FDM = 2 };
 enum { SEM_GUESS_ZERO = 0, SEM_GUESS_EXTRAPOLATE = 1, SEM_GUESS_LEARNED = 2 };
 
 typedef struct sem_ctx sem_ctx;
@@ -254,9 +257,10 @@ int sem_schrodinger_dirk4s3(sem_ctx* ctx, double* psi_re, double* psi_im, const 
  * No counterpart in the reference (its stage solves start from zero,
  * schrodinger.hpp:222,379).  A per-element network predicts the error of the
  * extrapolated stage guess 2 z^{n-1} - z^{n-2} from that guess's residual.
- * Rows are elements: input 4 N^2 BF16 features [r_re/s, r_im/s, alpha V,
- * mass/alpha] with s the element's RMS residual; output 2 N^2 FP32 values,
- * the correction (z - z_guess)/s.  Network: ReLU MLP d_in -> H -> H -> d_out,
+ * Rows are elements: input 4 N^2 BF16 features [r_re/rho, r_im/rho,
+ * alpha V, mass/alpha] with rho the element's RMS residual; output 2 N^2
+ * FP32 values, the correction (z - z_guess) mbar/rho with mbar the element's
+ * mean lumped mass.  Network: ReLU MLP d_in -> H -> H -> d_out,
  * BF16 tensor-core GEMMs with FP32 accumulation, FP32 master weights, Adam.
  * Weights W are [in][out] row-major FP32. */
 typedef struct sem_learner sem_learner;

@@ -104,7 +104,7 @@ SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
 OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE = 7, 8, 9
 PREC_FP64, PREC_MIXED = 0, 1
-PRECOND_NONE, PRECOND_DIAG = 0, 1
+PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2
 
 _lib = None

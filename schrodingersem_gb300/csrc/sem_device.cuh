@@ -390,6 +390,148 @@ __device__ __forceinline__ void apply_range(T* sm, int kmax, const Fac<T>& fac,
     __syncthreads();
 }
 
+// ------------------------------------- element fast-diagonalisation pass
+// Neumann-Neumann weight of an element-local copy: 1 / (number of elements
+// sharing the node); 0 on the Dirichlet boundary
+template <int N, typename T>
+__device__ __forceinline__ T nn_weight(const DevMesh& m, const NodeInfo& ni, int e)
+{
+    if (ni.kind == 0) return T(1);
+    if (ni_boundary(ni)) return T(0);
+    if (ni.kind == 1) return T(0.5);
+    const int node = __ldg(m.corner_node + 4 * e + ni.sc);
+    return T(1) / T(__ldg(m.node_ptr + node + 1) - __ldg(m.node_ptr + node));
+}
+
+template <typename T>
+__device__ inline const T* fdm_s(const DevMesh& m);
+template <>
+__device__ inline const double* fdm_s<double>(const DevMesh& m) { return m.fdmS64; }
+template <>
+__device__ inline const float* fdm_s<float>(const DevMesh& m) { return m.fdmS32; }
+template <typename T>
+__device__ inline const T* fdm_l(const DevMesh& m);
+template <>
+__device__ inline const double* fdm_l<double>(const DevMesh& m) { return m.fdmL64; }
+template <>
+__device__ inline const float* fdm_l<float>(const DevMesh& m) { return m.fdmL32; }
+
+// S and lambda of the mesh's degree into shared memory (every thread calls)
+template <int N, typename T>
+__device__ __forceinline__ void load_fdm_basis(T* S, T* lam, const DevMesh& m)
+{
+    const T* gs = fdm_s<T>(m);
+    const T* gl = fdm_l<T>(m);
+    for (int t = threadIdx.x; t < N * N; t += blockDim.x) S[t] = gs[t];
+    for (int t = threadIdx.x; t < N; t += blockDim.x) lam[t] = gl[t];
+}
+
+// One block-wide pass of the element preconditioner over [e0, e0+ne),
+// ne <= kmax, for the Schroedinger Res operator A = [M, aL; aL, -M]:
+//   z_e = (S x S) diag(1 / sqrt(m^2 + a^2 l_kl^2)) (S x S)^T r_e     per plane,
+//   l_kl = rx lambda_k + ry lambda_l,
+// the inverse of |A_e| for the element's rectangle approximation (half
+// widths ax, ay: mass m = ax ay, stiffness rx K (x) W + ry W (x) K with
+// rx = ay/ax, ry = ax/ay), in the basis that diagonalises the 1-D GLL
+// stiffness against the mass.  load(e,i,j,flat,u[NC]) supplies the
+// (weighted) input, store(e,i,j,flat,z[NC]) receives the element result.
+// Every thread of the block must call it.  S (S(i,k) at [i*N+k]) and lam
+// are in shared memory; the staging area sm uses the apply's u/f1 regions
+// (2 NC kmax N^2 values after the first N^2).
+template <int N, typename T, int NC, class Load, class Store>
+__device__ __forceinline__ void fdm_range(T* sm, int kmax, const T* S, const T* lam, const DevMesh& m, T alpha,
+                                          int e0, int ne, Load&& load, Store&& store)
+{
+    constexpr int NN = N * N;
+    const int total = ne * NN;
+    const int st = kmax * NN;
+    T* su = sm + NN;
+    T* stt = su + NC * st;
+    // 0. inputs
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int e = e0 + le;
+        T u[NC];
+        load(e, node % N, node / N, (long long)e * NN + node, u);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) su[c * st + t] = u[c];
+    }
+    __syncthreads();
+    // 1. t(a,j) = sum_i S(i,a) u(i,j)
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int a = node % N, j = node / N;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* uc = su + c * st + le * NN + j * N;
+            T acc = T(0);
+#pragma unroll
+            for (int i = 0; i < N; ++i) acc = fma(S[i * N + a], uc[i], acc);
+            stt[c * st + t] = acc;
+        }
+    }
+    __syncthreads();
+    // 2. u(a,b) = d(a,b) sum_j t(a,j) S(j,b)
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int a = node % N, b = node / N;
+        const float4 g = __ldg(m.fdm_el + e0 + le);
+        const T l = T(g.y) * lam[a] + T(g.z) * lam[b];
+        const T mm = T(g.x);
+        const T d = T(1) / sqrt(mm * mm + alpha * alpha * l * l);
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* tc = stt + c * st + le * NN + a;
+            T acc = T(0);
+#pragma unroll
+            for (int j = 0; j < N; ++j) acc = fma(tc[j * N], S[j * N + b], acc);
+            su[c * st + t] = d * acc;
+        }
+    }
+    __syncthreads();
+    // 3. t(i,b) = sum_a S(i,a) u(a,b)
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int i = node % N, b = node / N;
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* uc = su + c * st + le * NN + b * N;
+            T acc = T(0);
+#pragma unroll
+            for (int a = 0; a < N; ++a) acc = fma(S[i * N + a], uc[a], acc);
+            stt[c * st + t] = acc;
+        }
+    }
+    __syncthreads();
+    // 4. z(i,j) = sum_b t(i,b) S(j,b)
+#pragma unroll 4
+    for (int t = threadIdx.x; t < total; t += blockDim.x) {
+        const int le = t / NN;
+        const int node = t - le * NN;
+        const int i = node % N, j = node / N;
+        const int e = e0 + le;
+        T z[NC];
+#pragma unroll
+        for (int c = 0; c < NC; ++c) {
+            const T* tc = stt + c * st + le * NN + i;
+            T acc = T(0);
+#pragma unroll
+            for (int b = 0; b < N; ++b) acc = fma(tc[b * N], S[j * N + b], acc);
+            z[c] = acc;
+        }
+        store(e, i, j, (long long)e * NN + node, z);
+    }
+    __syncthreads();
+}
+
 // --------------------------------------------------------------- reductions
 // block sum of a double, result returned to every thread (fixed order)
 __device__ __forceinline__ double block_sum(double v, double* red)

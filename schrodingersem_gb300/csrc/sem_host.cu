@@ -222,6 +222,7 @@ struct sem_ctx {
     long long hist_steps = 0;
     int hist_stages = 0;
     double hist_dt = 0.0;
+    double hist_sig[2] = {0.0, 0.0};  // squared norms of the state the last call ended with
     // learned stage guess: network (owned by the caller) and the training
     // dataset recorded from solved stages (device workspace ds_X, ds_T)
     sem_learner* learner = nullptr;
@@ -297,6 +298,68 @@ static bool is_device_ptr(const void* p)
         return false;
     }
     return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+// Eigen-decomposition of a symmetric n x n matrix (row-major, overwritten):
+// cyclic Jacobi rotations (Golub & Van Loan, Matrix Computations, 8.5).  On
+// return A's diagonal holds the eigenvalues and V's columns the eigenvectors.
+static void sym_eig_jacobi(int n, std::vector<double>& A, std::vector<double>& V)
+{
+    V.assign((size_t)n * n, 0.0);
+    for (int i = 0; i < n; ++i) V[(size_t)i * n + i] = 1.0;
+    for (int sweep = 0; sweep < 100; ++sweep) {
+        double off = 0.0, diag = 0.0;
+        for (int p = 0; p < n; ++p) {
+            diag += A[(size_t)p * n + p] * A[(size_t)p * n + p];
+            for (int q = p + 1; q < n; ++q) off += A[(size_t)p * n + q] * A[(size_t)p * n + q];
+        }
+        if (off <= 1e-32 * diag) break;
+        for (int p = 0; p < n; ++p)
+            for (int q = p + 1; q < n; ++q) {
+                const double apq = A[(size_t)p * n + q];
+                if (apq == 0.0) continue;
+                const double theta = (A[(size_t)q * n + q] - A[(size_t)p * n + p]) / (2.0 * apq);
+                const double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double cs = 1.0 / std::sqrt(t * t + 1.0), sn = t * cs;
+                for (int k = 0; k < n; ++k) {  // columns p, q
+                    const double akp = A[(size_t)k * n + p], akq = A[(size_t)k * n + q];
+                    A[(size_t)k * n + p] = cs * akp - sn * akq;
+                    A[(size_t)k * n + q] = sn * akp + cs * akq;
+                }
+                for (int k = 0; k < n; ++k) {  // rows p, q
+                    const double apk = A[(size_t)p * n + k], aqk = A[(size_t)q * n + k];
+                    A[(size_t)p * n + k] = cs * apk - sn * aqk;
+                    A[(size_t)q * n + k] = sn * apk + cs * aqk;
+                }
+                for (int k = 0; k < n; ++k) {
+                    const double vkp = V[(size_t)k * n + p], vkq = V[(size_t)k * n + q];
+                    V[(size_t)k * n + p] = cs * vkp - sn * vkq;
+                    V[(size_t)k * n + q] = sn * vkp + cs * vkq;
+                }
+            }
+    }
+}
+
+// 1-D basis of the element preconditioner: K s = lambda W s for the GLL
+// stiffness K = D^T W D and mass W on [-1,1]; S(i,k) at [i*N+k] with
+// S^T W S = I, S^T K S = diag(lambda).  D column-major (D(i,j) at [i+j*N]).
+static void fdm_basis(int N, const std::vector<double>& w, const std::vector<double>& D, std::vector<double>& S,
+                      std::vector<double>& lam)
+{
+    std::vector<double> B((size_t)N * N), Q;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j) {
+            double k = 0.0;
+            for (int q = 0; q < N; ++q) k += D[q + (size_t)i * N] * w[q] * D[q + (size_t)j * N];
+            B[(size_t)i * N + j] = k / std::sqrt(w[i] * w[j]);
+        }
+    sym_eig_jacobi(N, B, Q);
+    S.assign((size_t)N * N, 0.0);
+    lam.assign(N, 0.0);
+    for (int k = 0; k < N; ++k) {
+        lam[k] = B[(size_t)k * N + k];
+        for (int i = 0; i < N; ++i) S[(size_t)i * N + k] = Q[(size_t)i * N + k] / std::sqrt(w[i]);
+    }
 }
 
 // Build topology (include/load_mesh.hpp:146-206) and metrics
@@ -491,6 +554,21 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
     };
     assemble(kloc, kdiag);
     assemble(ms, mdiag);
+    // element preconditioner data: 1-D basis and each element's rectangle
+    // approximation (half widths from the mean lengths of opposite sides)
+    std::vector<double> fS, fL;
+    fdm_basis(N, c->w, c->D, fS, fL);
+    std::vector<float4> fel(n_el);
+    for (int e = 0; e < n_el; ++e) {
+        double cx[4], cy[4];
+        for (int k = 0; k < 4; ++k) {
+            cx[k] = coords[2 * (size_t)elements[4 * (size_t)e + k]];
+            cy[k] = coords[2 * (size_t)elements[4 * (size_t)e + k] + 1];
+        }
+        auto len = [&](int a, int b) { return std::hypot(cx[b] - cx[a], cy[b] - cy[a]); };
+        const double ax = 0.25 * (len(0, 1) + len(3, 2)), ay = 0.25 * (len(0, 3) + len(1, 2));
+        fel[e] = make_float4((float)(ax * ay), (float)(ay / ax), (float)(ax / ay), 0.f);
+    }
 
     // device copies
     DevMesh& d = c->dm;
@@ -519,7 +597,9 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, g22, &d.g22)) || (s = upload(c, ms, &d.mass)) ||
         (s = upload(c, tof(g11), &d.g11f)) || (s = upload(c, tof(g12), &d.g12f)) ||
         (s = upload(c, tof(g22), &d.g22f)) || (s = upload(c, tof(ms), &d.massf)) ||
-        (s = upload(c, kdiag, &d.kdiag)) || (s = upload(c, mdiag, &d.mdiag)))
+        (s = upload(c, kdiag, &d.kdiag)) || (s = upload(c, mdiag, &d.mdiag)) ||
+        (s = upload(c, fS, &d.fdmS64)) || (s = upload(c, tof(fS), &d.fdmS32)) ||
+        (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)))
         return s;
     SEM_CUDA(cudaMallocHost((void**)&c->h_out, sizeof(SolveOut)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_sync, sizeof(GridSync)));
@@ -667,7 +747,8 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
             c->inner_fused = (int)v;
             return SEM_OK;
         case SEM_OPT_PRECOND:
-            if (v != SEM_PRECOND_NONE && v != SEM_PRECOND_DIAG) return fail(SEM_ERR_ARG, "bad preconditioner");
+            if (v != SEM_PRECOND_NONE && v != SEM_PRECOND_DIAG && v != SEM_PRECOND_FDM)
+                return fail(SEM_ERR_ARG, "bad preconditioner");
             c->precond = (int)v;
             return SEM_OK;
         case SEM_OPT_PROFILE:
@@ -809,10 +890,44 @@ extern "C" int sem_vec_axpby(sem_ctx* c, long long n, double a, const double* x,
 
 // --------------------------------------------------------- C ABI: operators
 // element-local op (input gathered with unmask semantics), then DSS + mask
+static bool overlap(const void* a, const void* b, size_t bytes)
+{
+    if (!a || !b) return false;
+    const char *x = (const char*)a, *y = (const char*)b;
+    return x < y + bytes && y < x + bytes;
+}
+
+// the apply may write its element-local result straight into the outputs and
+// assemble them in place when no output overlaps an input (the element
+// kernel gathers inputs across elements)
+static bool apply_direct(const sem_ctx* c, size_t word, const void* pot, const void* in0, const void* in1,
+                         const void* out0, const void* out1)
+{
+    const size_t b = word * (size_t)c->n;
+    const void* ins[3] = {pot, in0, in1};
+    const void* outs[2] = {out0, out1};
+    for (const void* o : outs)
+        for (const void* i : ins)
+            if (overlap(o, i, b)) return false;
+    return !overlap(out0, out1, b);
+}
+
 static int apply_galerkin(sem_ctx* c, int op, const double* pot, double alpha, const double* in0,
                           const double* in1, double* out0, double* out1, double scale = 1.0)
 {
     const int nc = (op == OP_RES || op == OP_F) ? 2 : 1;
+    if (scale == 1.0 && apply_direct(c, sizeof(double), pot, in0, in1, out0, nc == 2 ? out1 : nullptr)) {
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_apply<decltype(nv)::value>(c->dm, op, false, pot, alpha, in0, in1, out0, out1, true,
+                                                     c->stream);
+        }));
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_ring<decltype(nv)::value>(c->dm, false, DSS_MASK, out0, nc == 2 ? out1 : nullptr,
+                                                    c->stream);
+        }));
+        c->stats.fp64_applies++;
+        return SEM_OK;
+    }
     double* Y = nullptr;
     int s = wsget(c, "apply_Y", 2 * c->n, &Y);
     if (s) return s;
@@ -873,6 +988,16 @@ extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, 
 {
     SEM_CHECK_CTX(c);
     if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
+    if (apply_direct(c, sizeof(float), V, qr, qi, yr, yi)) {
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_apply<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true, c->stream);
+        }));
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_ring<decltype(nv)::value>(c->dm, true, DSS_MASK, yr, yi, c->stream);
+        }));
+        c->stats.fp32_applies++;
+        return SEM_OK;
+    }
     float* Y = nullptr;
     int s = wsget(c, "apply_Yf", 2 * c->n, &Y);
     if (s) return s;
@@ -972,7 +1097,11 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     if (c->inner_fused) {
         if ((s = wsget(c, "k32_AZ", v, &w.AZ)) || (s = wsget(c, "k32_Y3", v, &w.Y3))) return s;
     }
-    if (c->precond) {
+    if (c->precond == SEM_PRECOND_FDM && op == OP_RES) {
+        if ((s = wsget(c, "k32_Z0", v, &w.Z[0])) || (s = wsget(c, "k32_Z1", v, &w.Z[1]))) return s;
+        mx.fdm = 1;
+        mx.fused = 0;
+    } else if (c->precond) {
         float* pinv = nullptr;
         if ((s = wsget(c, "mx_pinv32", c->n, &pinv))) return s;
         k_prec<<<grid_1d(c->n), 256, 0, c->stream>>>(c->n, op, alpha, c->dm.mdiag, c->dm.kdiag, pot, pinv);
@@ -1444,8 +1573,18 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
                         c->prec == SEM_PREC_MIXED;
     // the stage history carries over from the previous driver call when it
     // continued the same kind of step (a wrong history only costs iterations:
-    // every stage is still solved to the same tolerance)
-    if (!extrap || c->hist_stages != stages || c->hist_dt != o->dt) c->hist_steps = 0;
+    // every stage is still solved to the same tolerance) and starts from the
+    // state that call ended with (same squared norms of both planes, bit for
+    // bit: the dots have a fixed summation order)
+    double sig[2] = {0.0, 0.0};
+    if (extrap) {
+        if ((s = dot_dev(c, r.P[r.cur], r.P[r.cur], &sig[0])) ||
+            (s = dot_dev(c, r.P[r.cur] + c->n, r.P[r.cur] + c->n, &sig[1])))
+            return s;
+    }
+    if (!extrap || c->hist_stages != stages || c->hist_dt != o->dt || sig[0] != c->hist_sig[0] ||
+        sig[1] != c->hist_sig[1])
+        c->hist_steps = 0;
     c->hist_stages = stages;
     c->hist_dt = o->dt;
     const long long hist0 = c->hist_steps;
@@ -1554,6 +1693,11 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             if ((s = schro_publish(&r))) return s;
             if (cb(user, step, psi_re, psi_im)) break;
         }
+    }
+    if (extrap && ok) {
+        if ((s = dot_dev(c, r.P[r.cur], r.P[r.cur], &c->hist_sig[0])) ||
+            (s = dot_dev(c, r.P[r.cur] + c->n, r.P[r.cur] + c->n, &c->hist_sig[1])))
+            return s;
     }
     if ((s = schro_publish(&r))) return s;
     *success = ok ? 1 : 0;

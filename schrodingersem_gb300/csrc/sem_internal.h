@@ -52,6 +52,15 @@ struct DevMesh {
     // premultiplied factors w_i w_j {A, B, C, J}
     const double *g11 = nullptr, *g12 = nullptr, *g22 = nullptr, *mass = nullptr;
     const float *g11f = nullptr, *g12f = nullptr, *g22f = nullptr, *massf = nullptr;
+    // element fast-diagonalisation preconditioner: 1-D GLL generalised
+    // eigenvectors S(i,k) at [i*N+k] (K s = lambda W s, S^T W S = I), their
+    // eigenvalues, and per element {ax ay, ay/ax, ax/ay, 0} of the element's
+    // rectangle approximation (half widths ax, ay)
+    const double* fdmS64 = nullptr;
+    const float* fdmS32 = nullptr;
+    const double* fdmL64 = nullptr;
+    const float* fdmL32 = nullptr;
+    const float4* fdm_el = nullptr;
 };
 
 // Grid barrier and error state of a persistent (cooperative) kernel.
@@ -81,6 +90,7 @@ struct KrylovWork {
     double* partials;  // [2 slots][grid][4]
     T* AZ;          // single-barrier MINRES: assembled A z_i (continuous format)
     T* Y3;          // single-barrier MINRES: y_i before the r2 correction
+    T* Z[2];        // element preconditioner: z = P^-1 r of the last two iterations
 };
 
 struct SolveArgs {
@@ -112,6 +122,7 @@ struct MixedArgs {
     float* x32[2];       // FP32 correction planes
     const float* pot32;  // FP32 copy of the potential (V or c)
     const float* pinv32; // diagonal preconditioner P^-1 (continuous format), or null
+    int fdm;             // element fast-diagonalisation preconditioner (Res only; uses KrylovWork::Z)
     int fused;           // inner solve with the single-barrier MINRES iteration (Res only)
     double outer_scale;  // refinement stops at |r| < outer_scale * (tol |r0| + tol)
 };
@@ -124,6 +135,10 @@ cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, d
 template <int N>
 cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
                        void* out, cudaStream_t st);
+// in-place assembly of element-local values touching only element rings
+// (k_ring); equals launch_dss with scale 1 into a separate output
+template <int N>
+cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, cudaStream_t st);
 template <int N>
 cudaError_t launch_unmask(const DevMesh& m, bool fp32, void* a, cudaStream_t st);
 template <int N>

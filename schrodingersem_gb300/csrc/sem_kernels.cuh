@@ -48,6 +48,81 @@ __global__ void k_dss(DevMesh m, const T* __restrict__ Y, T* __restrict__ out, T
     }
 }
 
+// In-place assembly of element-local values (the apply's own output) that
+// touches only the element rings.  Work items: every (element, side, k) for
+// k = 1..N-2, handled by the side's owner (interior sides) or its element
+// (boundary sides), then every corner node.  One item owns all copies of
+// its global node, so no two threads write the same copy.  Sums run in the
+// order dss_value uses (owner + other on sides; 0 + copies in
+// connected_elements order at corners), so the result equals
+// k_dss<MODE> with scale 1 bit for bit.  Element interiors are final as the
+// apply wrote them.
+template <int N, typename T, int MODE>
+__global__ void k_ring(DevMesh m, T* __restrict__ a0, T* __restrict__ a1)
+{
+    constexpr int NN = N * N;
+    constexpr int NS = N - 2;  // interior nodes per side
+    constexpr int NSd = NS > 0 ? NS : 1;
+    const long long n_side = (long long)m.E * 4 * NS;
+    const long long total = n_side + m.n_nodes;
+    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
+         it += (long long)gridDim.x * blockDim.x) {
+        if (it < n_side) {
+            const int e = (int)(it / (4 * NSd));
+            const int r = (int)(it - (long long)e * 4 * NSd);
+            const int sd = r / NSd, k = 1 + r % NSd;
+            const int fl = __ldg(m.flags + e);
+            const bool bnd = (fl >> (4 + sd)) & 1;
+            if (!bnd && !((fl >> sd) & 1)) continue;  // the neighbour owns this side
+            const int i = sd == 0 ? k : sd == 1 ? N - 1 : sd == 2 ? k : 0;
+            const int j = sd == 0 ? 0 : sd == 1 ? k : sd == 2 ? N - 1 : k;
+            const long long o = (long long)e * NN + j * N + i;
+            if (bnd) {
+                if (MODE != DSS_SUM) {
+                    a0[o] = T(0);
+                    if (a1) a1[o] = T(0);
+                }
+                continue;
+            }
+            const long long nf = (long long)__ldg(m.side_base + 4 * e + sd) + (long long)k * __ldg(m.side_step + 4 * e + sd);
+            T* planes[2] = {a0, a1};
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                T* a = planes[q];
+                if (!a) continue;
+                const T v = a[o] + a[nf];
+                a[o] = v;
+                a[nf] = MODE == DSS_MASK ? T(0) : v;
+            }
+        } else {
+            const int node = (int)(it - n_side);
+            const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
+            if (q1 <= q0) continue;
+            const long long f0 = __ldg(m.node_flat + q0);
+            const int e = (int)(f0 / NN);
+            const int loc = (int)(f0 - (long long)e * NN);
+            const int i = loc % N, j = loc / N;
+            const int c = (j == 0) ? (i == 0 ? 0 : 1) : (i == 0 ? 3 : 2);
+            const bool bnd = (__ldg(m.flags + e) >> (12 + c)) & 1;
+            T* planes[2] = {a0, a1};
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                T* a = planes[q];
+                if (!a) continue;
+                if (bnd) {
+                    if (MODE != DSS_SUM)
+                        for (int t = q0; t < q1; ++t) a[__ldg(m.node_flat + t)] = T(0);
+                    continue;
+                }
+                T sum = T(0);
+                for (int t = q0; t < q1; ++t) sum += a[__ldg(m.node_flat + t)];
+                for (int t = q0; t < q1; ++t)
+                    a[__ldg(m.node_flat + t)] = (MODE == DSS_MASK && t != q0) ? T(0) : sum;
+            }
+        }
+    }
+}
+
 // unmask in place: non-owner copies read owner copies, which are never written
 template <int N, typename T>
 __global__ void k_unmask(DevMesh m, T* a)
@@ -166,9 +241,12 @@ __global__ void k_resid_cont(DevMesh m, const double* __restrict__ b, const doub
     }
 }
 
-// One warp per element.  sigma_e = RMS of the residual over the element's
-// nodes (both planes); features (BF16, row e):
-//   [r_re / sigma, r_im / sigma, alpha V, (w_i w_j J) / alpha]   (4 N^2 values)
+// One warp per element.  rho_e = RMS of the residual over the element's
+// nodes (both planes), mbar_e = mean lumped mass w_i w_j J of the element;
+// features (BF16, row e):
+//   [r_re / rho, r_im / rho, alpha V, (w_i w_j J) / alpha]   (4 N^2 values)
+// and the element's solution scale sigma_e = rho_e / mbar_e (the size of
+// M^-1 r, the error a mass-dominated residual of size rho points to)
 template <int N>
 __global__ void k_features(DevMesh m, const double* __restrict__ r, const double* __restrict__ V, double alpha,
                            __nv_bfloat16* __restrict__ x, float* __restrict__ sigma)
@@ -179,15 +257,19 @@ __global__ void k_features(DevMesh m, const double* __restrict__ r, const double
     const int lane = threadIdx.x & 31;
     if (e >= m.E) return;
     const long long base = (long long)e * NN;
-    double s = 0.0;
+    double s = 0.0, ms = 0.0;
     for (int k = lane; k < NN; k += 32) {
         const double a = r[base + k], b = r[n + base + k];
         s += a * a + b * b;
+        ms += m.mass[base + k];
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    const double sg = sqrt(s / (2.0 * NN)) + 1e-300;
-    const double inv = 1.0 / sg;
+    for (int o = 16; o > 0; o >>= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, o);
+        ms += __shfl_xor_sync(0xffffffffu, ms, o);
+    }
+    const double rho = sqrt(s / (2.0 * NN)) + 1e-300;
+    const double inv = 1.0 / rho;
     __nv_bfloat16* row = x + (long long)e * 4 * NN;
     for (int k = lane; k < NN; k += 32) {
         row[k] = __float2bfloat16((float)(r[base + k] * inv));
@@ -195,7 +277,7 @@ __global__ void k_features(DevMesh m, const double* __restrict__ r, const double
         row[2 * NN + k] = __float2bfloat16((float)(alpha * V[base + k]));
         row[3 * NN + k] = __float2bfloat16((float)(m.mass[base + k] / alpha));
     }
-    if (lane == 0) sigma[e] = (float)sg;
+    if (lane == 0) sigma[e] = (float)(rho * NN / ms);
 }
 
 // training target of element e: (z - z_guess) / sigma_e at every node, with
@@ -358,6 +440,26 @@ cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl,
 }
 
 template <int N>
+cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, cudaStream_t st)
+{
+    const int tpb = 256;
+    const int grid = grid_for((long long)m.E * 4 * (N - 2) + m.n_nodes, tpb);
+#define SEM_RING_CASE(T)                                                                                  \
+    switch (mode) {                                                                                       \
+        case DSS_SUM: k_ring<N, T, DSS_SUM><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;             \
+        case DSS_MASK: k_ring<N, T, DSS_MASK><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;           \
+        default: k_ring<N, T, DSS_CONT><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;                 \
+    }
+    if (fp32) {
+        SEM_RING_CASE(float)
+    } else {
+        SEM_RING_CASE(double)
+    }
+#undef SEM_RING_CASE
+    return cudaGetLastError();
+}
+
+template <int N>
 cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
 {
     const int grid = grid_for(m.n, 256);
@@ -382,6 +484,7 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
                                           cudaStream_t);                                             \
     template cudaError_t launch_dss<NV>(const DevMesh&, bool, int, double, const void*, void*,       \
                                         cudaStream_t);                                               \
+    template cudaError_t launch_ring<NV>(const DevMesh&, bool, int, void*, void*, cudaStream_t);     \
     template cudaError_t launch_unmask<NV>(const DevMesh&, bool, void*, cudaStream_t);               \
     template cudaError_t launch_mask<NV>(const DevMesh&, bool, void*, cudaStream_t);                 \
     template cudaError_t launch_dot<NV>(const DevMesh&, const double*, const double*, double*, int,  \

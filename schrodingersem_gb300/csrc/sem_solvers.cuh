@@ -168,13 +168,14 @@ __device__ __forceinline__ void scal_givens(MinresScal<T>& sc, double alpha_i, d
 // Paige-Saunders form beta = sqrt(r2 . P^-1 r2).
 // rhs(ni, e, flat, c) gives the initial residual (continuous format) at a
 // node.  Returns false when a grid barrier timed out.
-template <int N, typename T, int OP, bool PRE, class Rhs>
+template <int N, typename T, int OP, int PRE, class Rhs>
 __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, MinresScal<T>& sc, const DevMesh& m,
                                             const T* pot, T alpha, int eb, int ee,
                                             const KrylovWork<T>& w, GridSync* gs, long long tmo,
                                             int& slot, Rhs&& rhs, T* const* xp, int maxit,
                                             double tol_rel, double tol_abs, MinresOut& res,
-                                            const T* __restrict__ pinv)
+                                            const T* __restrict__ pinv, const T* fS = nullptr,
+                                            const T* fL = nullptr)
 {
     constexpr int NN = N * N;
     constexpr int NC = op_nc<OP>();
@@ -195,34 +196,80 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
     };
     // P1: r; |r|^2 and r.z (z = P^-1 r); W[0] = W[1] = 0; Y[0] = A_local(z)
     T part = T(0), partz = T(0);
-    for (int e0 = eb; e0 < ee; e0 += kmax)
-        apply_range<N, T, OP>(
-            sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
-            [&](int e, int i, int j, long long flat, T* u) {
-                const NodeInfo ni = node_info<N>(m, e, i, j);
-                const bool own = ni_owner(ni);
-                const T pv = PRE ? pinv[flat] : T(1);
+    if constexpr (PRE == 2) {
+        // element preconditioner: weighted local solves into Y[1], then
+        // z = DSS (continuous) kept in Z[0]
+        T* Zl = w.Y[1];
+        for (int e0 = eb; e0 < ee; e0 += kmax)
+            fdm_range<N, T, NC>(
+                sm, kmax, fS, fL, m, alpha, e0, min(kmax, ee - e0),
+                [&](int e, int i, int j, long long flat, T* u) {
+                    const NodeInfo ni = node_info<N>(m, e, i, j);
+                    const bool own = ni_owner(ni);
+                    const T wt = nn_weight<N, T>(m, ni, e);
 #pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    const T r = rhs(ni, e, flat, c);
-                    L[ir2][c * n + flat] = r;
-                    W[iw1][c * n + flat] = T(0);
-                    W[iw2][c * n + flat] = T(0);
-                    const T z = PRE ? pv * r : r;
-                    u[c] = z;
-                    if (own) {
-                        part = fma(r, r, part);
-                        partz = fma(r, z, partz);
+                    for (int c = 0; c < NC; ++c) {
+                        const T r = rhs(ni, e, flat, c);
+                        L[ir2][c * n + flat] = r;
+                        W[iw1][c * n + flat] = T(0);
+                        W[iw2][c * n + flat] = T(0);
+                        u[c] = wt * r;
+                        if (own) part = fma(r, r, part);
                     }
-                }
-            },
-            store_y(w.Y[0]));
+                },
+                [&](int e, int i, int j, long long flat, const T* z) {
+                    const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) Zl[c * n + flat] = wt * z[c];
+                });
+        if (!grid_barrier(gs, tmo)) return false;
+        for (int e0 = eb; e0 < ee; e0 += kmax)
+            apply_range<N, T, OP>(
+                sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+                [&](int e, int i, int j, long long flat, T* u) {
+                    const NodeInfo ni = node_info<N>(m, e, i, j);
+                    const bool own = ni_owner(ni);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const T z = dss_value<N, T, DSS_CONT>(m, Zl + c * n, ni, e, flat);
+                        w.Z[0][c * n + flat] = z;
+                        u[c] = z;
+                        if (own) partz = fma(L[ir2][c * n + flat], z, partz);
+                    }
+                },
+                store_y(w.Y[0]));
+    } else {
+        for (int e0 = eb; e0 < ee; e0 += kmax)
+            apply_range<N, T, OP>(
+                sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+                [&](int e, int i, int j, long long flat, T* u) {
+                    const NodeInfo ni = node_info<N>(m, e, i, j);
+                    const bool own = ni_owner(ni);
+                    const T pv = PRE == 1 ? pinv[flat] : T(1);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const T r = rhs(ni, e, flat, c);
+                        L[ir2][c * n + flat] = r;
+                        W[iw1][c * n + flat] = T(0);
+                        W[iw2][c * n + flat] = T(0);
+                        const T z = PRE == 1 ? pv * r : r;
+                        u[c] = z;
+                        if (own) {
+                            part = fma(r, r, part);
+                            partz = fma(r, z, partz);
+                        }
+                    }
+                },
+                store_y(w.Y[0]));
+    }
     double bb = 0.0, bz = 0.0;
     grid_sum2_t<T>(part, partz, w.partials, slot, gs, tmo, red, ok, bb, bz);
     slot ^= 1;
     if (!ok) return false;
     if (threadIdx.x == 0) {
-        scal_init(sc, sqrt(bb), sqrt(bz));  // minres.hpp:28,31
+        // minres.hpp:28,31; preconditioned runs measure the stop relative to
+        // the preconditioned norm sqrt(r.P^-1 r) their phibar estimates
+        scal_init(sc, PRE ? sqrt(bz) : sqrt(bb), sqrt(bz));
         scal_publish(sc, 1, 0.0);
     }
     __syncthreads();
@@ -241,7 +288,7 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                 const int node = (int)(idx - (long long)e * NN);
                 const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
                 const bool own = ni_owner(ni);
-                const T pv = PRE ? pinv[idx] : T(1);
+                const T pv = PRE == 1 ? pinv[idx] : T(1);
 #pragma unroll
                 for (int c = 0; c < NC; ++c) {
                     const long long q = c * n + idx;
@@ -252,11 +299,11 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                         r1v = L[ir1][q];
                         y3 = av - c1 * r1v;
                     }
-                    const T vv = inv_b * (PRE ? pv * L[ir2][q] : L[ir2][q]);
+                    const T vv = inv_b * (PRE == 2 ? w.Z[(it - 1) & 1][q] : PRE == 1 ? pv * L[ir2][q] : L[ir2][q]);
                     if (own) s1 = fma(vv, y3, s1);
                     L[iy][q] = y3;
                     if (pending) {
-                        const T vprev = tpinvb * (PRE ? pv * r1v : r1v);
+                        const T vprev = tpinvb * (PRE == 2 ? w.Z[it & 1][q] : PRE == 1 ? pv * r1v : r1v);
                         const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
                         W[iw][q] = wn;
                         if (own) xp[c][idx] += tpphi * wn;
@@ -283,23 +330,65 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
             const T c2 = sc.c2;
             T ss = T(0);
             T* Ynext = w.Y[it & 1];
-            for (int e0 = eb; e0 < ee; e0 += kmax)
-                apply_range<N, T, OP>(
-                    sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
-                    [&](int e, int i, int j, long long flat, T* u) {
-                        const bool own = ni_owner(node_info<N>(m, e, i, j));
-                        const T pv = PRE ? pinv[flat] : T(1);
+            if constexpr (PRE == 2) {
+                // y5 and its weighted local solves (into Y[it-1], read in
+                // Phase B above); after the barrier z = DSS -> Z[it & 1]
+                T* Zl = w.Y[(it - 1) & 1];
+                for (int e0 = eb; e0 < ee; e0 += kmax)
+                    fdm_range<N, T, NC>(
+                        sm, kmax, fS, fL, m, alpha, e0, min(kmax, ee - e0),
+                        [&](int e, int i, int j, long long flat, T* u) {
+                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
 #pragma unroll
-                        for (int c = 0; c < NC; ++c) {
-                            const long long q = c * n + flat;
-                            const T y5 = L[iy][q] - c2 * L[ir2][q];
-                            L[iy][q] = y5;
-                            const T z = PRE ? pv * y5 : y5;  // y = precond(r2), minres.hpp:60
-                            u[c] = z;
-                            if (own) ss = fma(y5, z, ss);
-                        }
-                    },
-                    store_y(Ynext));
+                            for (int c = 0; c < NC; ++c) {
+                                const long long q = c * n + flat;
+                                const T y5 = L[iy][q] - c2 * L[ir2][q];
+                                L[iy][q] = y5;
+                                u[c] = wt * y5;
+                            }
+                        },
+                        [&](int e, int i, int j, long long flat, const T* z) {
+                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) Zl[c * n + flat] = wt * z[c];
+                        });
+                if (!grid_barrier(gs, tmo)) return false;
+                T* Zn = w.Z[it & 1];
+                for (int e0 = eb; e0 < ee; e0 += kmax)
+                    apply_range<N, T, OP>(
+                        sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+                        [&](int e, int i, int j, long long flat, T* u) {
+                            const NodeInfo ni = node_info<N>(m, e, i, j);
+                            const bool own = ni_owner(ni);
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) {
+                                const long long q = c * n + flat;
+                                const T z = dss_value<N, T, DSS_CONT>(m, Zl + c * n, ni, e, flat);
+                                Zn[q] = z;
+                                u[c] = z;
+                                if (own) ss = fma(L[iy][q], z, ss);
+                            }
+                        },
+                        store_y(Ynext));
+            } else {
+                for (int e0 = eb; e0 < ee; e0 += kmax)
+                    apply_range<N, T, OP>(
+                        sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
+                        [&](int e, int i, int j, long long flat, T* u) {
+                            const bool own = ni_owner(node_info<N>(m, e, i, j));
+                            const T pv = PRE == 1 ? pinv[flat] : T(1);
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) {
+                                const long long q = c * n + flat;
+                                const T y5 = L[iy][q] - c2 * L[ir2][q];
+                                L[iy][q] = y5;
+                                const T z = PRE == 1 ? pv * y5 : y5;  // y = precond(r2), minres.hpp:60
+                                u[c] = z;
+                                if (own) ss = fma(y5, z, ss);
+                            }
+                        },
+                        store_y(Ynext));
+            }
             double bnew2 = 0.0;
             grid_sum2_t<T>(ss, T(0), w.partials, slot, gs, tmo, red, ok, bnew2, dummy);
             slot ^= 1;
@@ -326,11 +415,11 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
             const int node = (int)(idx - (long long)e * NN);
             const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
             if (!ni_owner(ni)) continue;
-            const T pv = PRE ? pinv[idx] : T(1);
+            const T pv = PRE == 1 ? pinv[idx] : T(1);
 #pragma unroll
             for (int c = 0; c < NC; ++c) {
                 const long long q = c * n + idx;
-                const T vprev = tpinvb * (PRE ? pv * L[ir1][q] : L[ir1][q]);
+                const T vprev = tpinvb * (PRE == 2 ? w.Z[(it - 1) & 1][q] : PRE == 1 ? pv * L[ir1][q] : L[ir1][q]);
                 const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
                 xp[c][idx] += tpphi * wn;
             }
@@ -412,7 +501,7 @@ __device__ __forceinline__ bool minres_core_fused(T* sm, int kmax, double* red, 
     slot ^= 1;
     if (!ok) return false;
     if (threadIdx.x == 0) {
-        scal_init(sc, sqrt(bb), sqrt(bz));
+        scal_init(sc, PRE ? sqrt(bz) : sqrt(bb), sqrt(bz));  // as minres_core
         scal_publish(sc, 1, 0.0);
     }
     __syncthreads();
@@ -574,7 +663,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         return r;
     };
     MinresOut r{};
-    if (!minres_core<N, T, OP, false>(sm, kmax, red, sc, m, pot, alpha, eb, ee, w, a.sync, a.timeout_ns, slot,
+    if (!minres_core<N, T, OP, 0>(sm, kmax, red, sc, m, pot, alpha, eb, ee, w, a.sync, a.timeout_ns, slot,
                                       rhs, xp, a.maxit, a.tol, a.tol, r, (const T*)nullptr))
         return;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -602,6 +691,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
     __shared__ double red[34];
     __shared__ MinresScal<float> sc;
     __shared__ double sweep_state[3];  // r0, |r|, done
+    __shared__ float fdmS[NN], fdmL[N];  // element preconditioner basis
     double* sm64 = (double*)smraw;
     float* sm32 = (float*)smraw;
     const Fac<double> fac64 = fac_of<double>(m);
@@ -677,13 +767,24 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         }
         // ---- FP32 inner solve A d = r (relative tolerance inner_tol)
         load_dmat_raw<N, float>(sm32, m);
+        if (OP == OP_RES && mx.fdm) load_fdm_basis<N, float>(fdmS, fdmL, m);
         __syncthreads();
         const double* r64c[2] = {mx.r64[0], mx.r64[1]};
         auto rhs = [&](const NodeInfo&, int, long long flat, int c) -> float { return (float)r64c[c][flat]; };
         MinresOut ir{};
         const int budget = min(mx.inner_maxit, a.maxit - inner_total);
-        bool okc;
-        if (OP == OP_RES && mx.fused)
+        bool okc = false;
+        bool done_fdm = false;
+        if constexpr (OP == OP_RES) {
+            if (mx.fdm) {
+                okc = minres_core<N, float, OP, 2>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee, w,
+                                                   a.sync, a.timeout_ns, slot, rhs, mx.x32, budget, mx.inner_tol,
+                                                   0.0, ir, (const float*)nullptr, fdmS, fdmL);
+                done_fdm = true;
+            }
+        }
+        if (done_fdm) {
+        } else if (OP == OP_RES && mx.fused)
             okc = mx.pinv32
                       ? minres_core_fused<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb,
                                                               ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
@@ -693,10 +794,10 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
                                                                budget, mx.inner_tol, 0.0, ir, (const float*)nullptr);
         else
             okc = mx.pinv32
-                      ? minres_core<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
+                      ? minres_core<N, float, OP, 1>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
                                                         w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
                                                         mx.inner_tol, 0.0, ir, mx.pinv32)
-                      : minres_core<N, float, OP, false>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
+                      : minres_core<N, float, OP, 0>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
                                                          w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
                                                          mx.inner_tol, 0.0, ir, (const float*)nullptr);
         if (!okc) return;

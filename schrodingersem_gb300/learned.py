@@ -7,9 +7,10 @@ on the GPU in the library's own kernels.  torch tensors only carry device
 memory in and out.
 
 Rows are elements.  Input row (4 N^2 BF16 values): the residual of the
-extrapolated stage guess scaled by the element's RMS residual s (real and
+extrapolated stage guess scaled by the element's RMS residual rho (real and
 imaginary planes), alpha V and the lumped mass over alpha.  Output row
-(2 N^2): the predicted correction (z - z_guess)/s.  ``Context.record``
+(2 N^2): the predicted correction (z - z_guess) mbar / rho, mbar the
+element's mean lumped mass.  ``Context.record``
 collects such rows from solved stages; ``Learner.fit`` trains on them;
 ``Context.set_learner`` makes the drivers use the network, with the
 extrapolation kept whenever the network's guess has the larger FP64
