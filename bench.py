@@ -38,6 +38,7 @@ WORKLOAD = ("Schroedinger SDIRK4-3 time step, 64x64 jittered quads on [-8,8]^2 (
             "(263,169 nodes), V=(x^2+y^2)/2, Gaussian packet sigma=1 r0=(-2,0) k=(3,0), dt=1e-2, "
             "MINRES tol 1e-10")
 DT, TOL, P, NEL = 1e-2, 1e-10, 8, 64
+ORACLE_TOL = 1e-13  # MINRES tolerance of the FP64 accuracy reference run
 
 
 def workload_inputs():
@@ -242,17 +243,24 @@ FORMS = {
                                        "extrapolated linearly from the last two steps (test relative to |b|)"),
     "mixed_diag_extrap": ("mixed", 1e-4, 1, "FP32-inner MINRES with diagonal preconditioner in FP64 iterative "
                                             "refinement, extrapolated stage guess (test relative to |b|)"),
+    "mixed_fdm": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation |A|^-1 "
+                                    "preconditioner in FP64 iterative refinement, zero stage guess"),
+    "mixed_fdm_extrap": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+                                           "preconditioner in FP64 iterative refinement, extrapolated stage "
+                                           "guess (test relative to |b|)"),
+    "mixed_fdm_learned": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+                                            "preconditioner in FP64 iterative refinement, stage guess = "
+                                            "extrapolation corrected by the BF16 network (trained on the GPU on "
+                                            "stage solves of other initial packets), residual-minimising step"),
 }
-FORMS["mixed_fdm"] = ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation |A|^-1 "
-                                        "preconditioner in FP64 iterative refinement, zero stage guess")
-FORMS["mixed_fdm_extrap"] = ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
-                                               "preconditioner in FP64 iterative refinement, extrapolated stage "
-                                               "guess (test relative to |b|)")
-GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1}
+GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1, "mixed_fdm_learned": 2}
+# training trajectories of the learned form: packets (centre, sigma, momentum)
+# other than the workload's, on the same mesh and potential
+TRAIN_PACKETS = [((-3.0, 1.0), 1.2, (2.0, 1.0)), ((1.0, -2.0), 0.8, (-2.5, 2.0)), ((0.5, 2.5), 1.0, (1.0, -3.0))]
+TRAIN_STEPS = 10
 
 
-def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
-    """warm-up + timed steps of one solver form, state resident in HBM"""
+def set_form_options(ctx, form):
     from schrodingersem_gb300 import capi
     prec, itol, pc, _ = FORMS[form]
     ctx.set_option(capi.OPT_PRECOND, pc)
@@ -265,10 +273,55 @@ def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
     ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64)
     if itol:
         ctx.set_option(capi.OPT_INNER_TOL, itol)
+
+
+def train_learner(ctx, torch, Vd, X, Y):
+    """record stage solves of TRAIN_PACKETS (extrapolated guesses), fit the
+    network on them; returns the learner and a summary"""
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.learned import Learner
+    from schrodingersem_gb300.meshgen import gaussian_packet
+    t0 = time.time()
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_EXTRAPOLATE)
+    ctx.record(ctx.E * 3 * (TRAIN_STEPS - 2) * len(TRAIN_PACKETS))
+    dtr = DT / 2.0
+    J, _, _, _ = ctx.metrics()
+    _, w, _ = ctx.quadrature()
+    for c, sg, k in TRAIN_PACKETS:
+        re, im = gaussian_packet(X, Y, c, sg, k)
+        nrm = mass_norm(J, w, re, im)
+        dre, dim = ctx.to_device(re / nrm), ctx.to_device(-im / nrm)
+        if not ctx.schrodinger("dirk4s3", dre, dim, Vd, (TRAIN_STEPS - 0.5) * dtr, dtr, 20 * ctx.dof(), TOL):
+            raise RuntimeError("training trajectory did not converge")
+    torch.cuda.synchronize()
+    t_rec = time.time() - t0
+    Xd, Td = ctx.dataset()
+    ctx.record(0)
+    t1 = time.time()
+    L = Learner.for_mesh(ctx.N, hidden=256, seed=3)
+    loss = L.fit(Xd, Td, epochs=4, batch=1024, lr=1e-3, seed=11)
+    torch.cuda.synchronize()
+    t_fit = time.time() - t1
+    tv = float(Td.float().pow(2).mean())
+    ctx.set_learner(L)
+    return L, {"rows": int(Xd.shape[0]), "record_s": t_rec, "fit_s": t_fit, "final_mse": loss,
+               "final_mse_rel": loss / tv if tv > 0 else None, "params": int(
+                   L.d_in * L.hidden + L.hidden + L.hidden * L.hidden + L.hidden + L.hidden * L.d_out + L.d_out)}
+
+
+def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
+    """warm-up + timed steps of one solver form, state resident in HBM"""
+    from schrodingersem_gb300 import capi
+    set_form_options(ctx, form)
     dtr = DT / 2.0
     maxit = 20 * ctx.dof()
     dre, dim, dV = ctx.to_device(re), ctx.to_device(im), ctx.to_device(Vr)
     st = torch.cuda.current_stream()
+    training = None
+    if GUESS.get(form, 0) == 2:  # untimed: record training trajectories, fit the network
+        X, Y = ctx.node_coords()
+        _, training = train_learner(ctx, torch, dV, X, Y)
+        set_form_options(ctx, form)
 
     def one_step(pr, pi, V):
         if not ctx.schrodinger("dirk4s3", pr, pi, V, 0.5 * dtr, dtr, maxit, TOL):
@@ -301,6 +354,10 @@ def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
         "it64": s1.solver_iterations_fp64 - s0.solver_iterations_fp64,
         "it32": s1.solver_iterations_fp32 - s0.solver_iterations_fp32,
         "applies64": s1.fp64_applies - s0.fp64_applies,
+        "learned": ({"guesses": s1.learned_guesses - s0.learned_guesses,
+                     "accepted": s1.learned_accepted - s0.learned_accepted,
+                     "last_residual_ratio": s1.last_guess_residual_ratio, "last_theta": s1.last_guess_theta,
+                     "training": training} if training else None),
         "one_step": one_step,
     }
 
@@ -340,6 +397,17 @@ def run_ours(args):
     Vr = X * X + Y * Y                               # V' = 2 * (x^2+y^2)/2
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     forms = [f for f in args.forms.split(",") if f]
+    # accuracy reference: the same number of steps by the plain FP64 solver at
+    # MINRES tolerance 1e-13 (untimed); every form is judged against it
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_FP64)
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_ZERO)
+    o_re, o_im = ctx.to_device(re), ctx.to_device(im)
+    dVo = ctx.to_device(Vr)
+    for _ in range(args.warmup + args.steps):
+        if not ctx.schrodinger("dirk4s3", o_re, o_im, dVo, 0.25 * DT, 0.5 * DT, 40 * ctx.dof(), ORACLE_TOL):
+            raise RuntimeError("FP64 reference run did not converge")
+    oracle_state = (o_re.cpu().numpy(), o_im.cpu().numpy())
+    del o_re, o_im, dVo
     res = {}
     with ClockSampler(local) as clk:
         if dist:
@@ -348,15 +416,16 @@ def run_ours(args):
             res[f] = run_form(ctx, torch, f, re, im, Vr, args.steps, args.warmup, flush)
         if dist:
             dist.barrier()
-    # accuracy of every form against the plain FP64 solve (M-weighted L2)
-    ref_state = res["fp64"]["state"] if "fp64" in res else None
+    # accuracy of every form (M-weighted relative L2) against the FP64
+    # reference run, and against the plain FP64 form at the workload tolerance
+    def rel(a, b):
+        return mass_norm(J, w, a[0] - b[0], a[1] - b[1]) / mass_norm(J, w, *b)
+
     for f, r in res.items():
-        if ref_state is None:
-            r["rel_err_vs_fp64"] = None
-            continue
-        dr, di = r["state"][0] - ref_state[0], r["state"][1] - ref_state[1]
-        r["rel_err_vs_fp64"] = mass_norm(J, w, dr, di) / mass_norm(J, w, *ref_state)
-    valid = [f for f in forms if res[f]["rel_err_vs_fp64"] is None or res[f]["rel_err_vs_fp64"] <= 1e-8]
+        r["rel_err_vs_fp64"] = rel(r["state"], oracle_state)
+        r["rel_err_vs_plain_fp64"] = rel(r["state"], res["fp64"]["state"]) if "fp64" in res else None
+        r["norm_drift"] = abs(mass_norm(J, w, *r["state"]) - 1.0)
+    valid = [f for f in forms if res[f]["rel_err_vs_fp64"] <= 1e-8]
     head = min(valid, key=lambda f: res[f]["ms"])
     H = res[head]
     ms = H["ms"]
@@ -370,7 +439,7 @@ def run_ours(args):
     h_im = torch.from_numpy(im.copy()).pin_memory()
     h_V = torch.from_numpy(np.ascontiguousarray(Vr)).pin_memory()
     prec = FORMS[head][0]
-    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED if prec == "mixed" else capi.PREC_FP64)
+    set_form_options(ctx, head)
     st = torch.cuda.current_stream()
     for _ in range(min(2, args.warmup)):
         H["one_step"](h_re.numpy(), h_im.numpy(), h_V.numpy())
@@ -393,14 +462,21 @@ def run_ours(args):
     # per Krylov iteration one Res apply (9 words/node) + 13 two-plane vector
     # words; per FP64 refinement sweep one FP64 residual (apply + 5 words)
     n = ctx.n
-    b64, b32 = n * 8 * (9 + 26), n * 4 * (9 + 26)
+    # (with the element preconditioner 16 two-plane vector words instead of
+    # 13: its local solve reads y, r2 and writes y and the local result; the
+    # apply pass reads that, writes z and reads y for beta; Phase B reads z
+    # instead of r2 and the previous z instead of r1)
+    b64 = n * 8 * (9 + 26)
+    b32 = n * 4 * (9 + (32 if FORMS[head][2] == 2 else 26))
     sweeps_total = H["applies64"] if prec == "mixed" else 0
     alg_bytes = H["it64"] * b64 + H["it32"] * b32 + sweeps_total * n * 8 * 14
     achieved = alg_bytes / (H["solver_ms"] / 1e3) / 1e9 if H["solver_ms"] > 0 else None
     kern = "k_minres_mixed<9,RES>" if prec == "mixed" else "k_minres<9,double,RES>"
     forms_out = {f: {"s_per_step": r["ms"] / 1e3, "minres_iters_per_stage": r["iters_per_stage"],
                      "refine_sweeps_per_stage": r["sweeps_per_stage"], "rel_err_vs_fp64": r["rel_err_vs_fp64"],
-                     "description": FORMS[f][3]} for f, r in res.items()}
+                     "rel_err_vs_plain_fp64": r["rel_err_vs_plain_fp64"], "norm_drift": r["norm_drift"],
+                     "description": FORMS[f][3], **({"learned": r["learned"]} if r.get("learned") else {})}
+                 for f, r in res.items()}
     cpu = cpu_baseline_sample(res["fp64"]["iters_per_step"] if "fp64" in res else H["iters_per_step"]) \
         if not args.no_cpu else None
     flops64 = n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
@@ -409,6 +485,8 @@ def run_ours(args):
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f64+f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "form": FORMS[head][3],
+                   "accuracy": f"M-weighted relative L2 of the state after warm-up + timed steps against the FP64 "
+                               f"solver at MINRES tolerance {ORACLE_TOL:g} (headline forms must stay within 1e-8)",
                    "l2": "flushed before every step (256 MiB write)", "parallelism": "replicas only"},
         "forms": forms_out,
         "speedup_vs_plain_fp64": (res["fp64"]["ms"] / ms) if "fp64" in res else None,
@@ -441,7 +519,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--forms", default="fp64,mixed,mixed_diag,mixed_fdm,mixed_fdm_extrap",
+    ap.add_argument("--forms", default="fp64,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_learned",
                     help="solver forms to time (comma list)")
     args = ap.parse_args()
     if args.impl == "reference":

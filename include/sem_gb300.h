@@ -72,8 +72,14 @@ enum sem_option {
     SEM_OPT_INNER_ITERATION = 8, /* FP32 inner MINRES iteration for Res: 1 (default) one grid
                                     barrier per iteration (operator product carried by
                                     recurrence), 0 the two-barrier form of the FP64 solver */
-    SEM_OPT_REFINE_TOL_SCALE = 9 /* mixed mode stops at |r| < s (tol |r0| + tol), s in (0,1],
+    SEM_OPT_REFINE_TOL_SCALE = 9, /* mixed mode stops at |r| < s (tol |r0| + tol), s in (0,1],
                                     default 1 (the reference's test on the true residual) */
+    SEM_OPT_APPLY_PIPELINE = 10  /* FP32 standalone apply: 1 (default) bulk-copy pipelined element
+                                    kernel when the input fields are 16-byte aligned, 0 the
+                                    one-pass kernel; same results bit for bit.  A pipelined
+                                    apply whose bounded wait expired is reported as
+                                    SEM_ERR_DEVICE_WAIT by the next sem_dot, solver or
+                                    driver call */
 };
 enum { SEM_PREC_FP64 = 0, SEM_PREC_MIXED = 1 };
 enum { SEM_PRECOND_NONE = 0, SEM_PRECOND_DIAG = 1, SEM_PRECOND_FDM = 2 };
@@ -119,8 +125,9 @@ typedef struct {
     long long solver_iterations_fp64; /* Krylov iterations run in FP64 */
     long long solver_iterations_fp32; /* Krylov iterations run in FP32 */
     long long learned_guesses;      /* stage guesses the learned model proposed */
-    long long learned_accepted;     /* ... and that beat the extrapolation's residual */
+    long long learned_accepted;     /* ... and that lowered the extrapolation's residual */
     double last_guess_residual_ratio; /* |r(guess used)| / |r(extrapolated)| of the last such stage */
+    double last_guess_theta;        /* step taken along the predicted correction (1: as predicted) */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop
@@ -288,8 +295,10 @@ int sem_learner_fit(sem_learner* learner, const void* X, const float* T, long lo
 int sem_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, void* cuda_stream);
 /* network used by the SDIRK drivers when SEM_OPT_STAGE_GUESS is
  * SEM_GUESS_LEARNED in mixed precision (NULL: extrapolation only).  The
- * caller keeps ownership.  Every proposed guess is checked: the driver keeps
- * the extrapolation when the network's guess has the larger FP64 residual. */
+ * caller keeps ownership.  Every proposed guess is checked in FP64: the
+ * driver moves from the extrapolation along the predicted correction by the
+ * step that minimises the residual norm (the extrapolation itself when no
+ * positive step lowers it). */
 int sem_ctx_set_learner(sem_ctx* ctx, sem_learner* learner);
 /* record training rows from the SDIRK drivers' stage solves (mixed precision,
  * SEM_GUESS_EXTRAPOLATE or _LEARNED, from the third step on) into a device

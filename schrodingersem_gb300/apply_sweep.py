@@ -53,6 +53,7 @@ def main():
     ap.add_argument("--p", default="2-16")
     ap.add_argument("--prec", default="fp32,fp64")
     ap.add_argument("--reps", type=int, default=10)
+    ap.add_argument("--pipeline", type=int, default=1, help="1: bulk-copy pipelined kernel, 0: one-pass kernel")
     a = ap.parse_args()
     import torch
 
@@ -65,6 +66,8 @@ def main():
         n = max(2, int(round(math.sqrt(a.nodes) / p)))
         co, el = structured_quads(n, box=(-12.0, 12.0, -12.0, 12.0), jitter=0.1, seed=1)
         ctx = S.Context(p, coords=co, elements=el)
+        from schrodingersem_gb300 import capi
+        ctx.set_option(capi.OPT_APPLY_PIPELINE, a.pipeline)
         for prec in a.prec.split(","):
             dt, s = (torch.float64, 8) if prec == "fp64" else (torch.float32, 4)
             g = torch.Generator(device="cuda").manual_seed(p)
@@ -87,7 +90,7 @@ def main():
             nbytes = ctx.n * s * 9
             gbs = nbytes / ms / 1e6
             print(json.dumps({"p": p, "n": n, "elements": ctx.E, "global_nodes": ctx.info.n_nodes,
-                              "n_loc": ctx.n, "prec": prec, "ms": round(ms, 4), "bytes": nbytes,
+                              "n_loc": ctx.n, "prec": prec, "pipeline": a.pipeline, "ms": round(ms, 4), "bytes": nbytes,
                               "gbs": round(gbs, 1), "frac_hbm": round(gbs / peak, 4), "peak_source": src}),
                   flush=True)
             del q, yr, yi

@@ -38,7 +38,8 @@ class SemStats(C.Structure):
                 ("kernel_launches", C.c_longlong), ("solver_launches", C.c_longlong),
                 ("solver_kernel_ms", C.c_double), ("solver_iterations_fp64", C.c_longlong),
                 ("solver_iterations_fp32", C.c_longlong), ("learned_guesses", C.c_longlong),
-                ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double)]
+                ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double),
+                ("last_guess_theta", C.c_double)]
 
 
 STEP_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, _dp, _dp)
@@ -102,7 +103,7 @@ SIGNATURES = {
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
-OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE = 7, 8, 9
+OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE = 7, 8, 9, 10
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

@@ -1,0 +1,478 @@
+// Pipelined element operator for the standalone applies.
+//
+// A persistent grid walks the mesh in batches of K elements (K N^2 nodes,
+// contiguous in every field).  For each batch one thread issues a 1-D bulk
+// copy (cp.async.bulk, completion counted on an mbarrier) of every array the
+// operator reads -- the inputs, the premultiplied factors, the potential --
+// into one of S shared-memory stages, so S batches of loads are in flight
+// per block while the block computes on the oldest.  Inputs in the masked
+// format are then patched at the ring copies that are not the owner (their
+// value is read from the owner copy, the reference's unmask), the two
+// contraction phases run from shared memory, and the element-local result
+// is stored with coalesced stores.  A batch shorter than K (the mesh tail)
+// is loaded with plain loads instead: bulk copies need 16-byte sizes.
+//
+// Every wait on an mbarrier is bounded (globaltimer); on expiry the block
+// records an error in DevMesh::dev_err, waits (bounded) for its own copies
+// in flight and returns.
+#pragma once
+#include <cstdint>
+
+#include "sem_device.cuh"
+
+namespace semgb {
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_fence_init()
+{
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// arrive (count 1) and add `bytes` to the transaction count of this phase
+__device__ __forceinline__ void mbar_arrive_tx(uint64_t* bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity)
+{
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// wait for phase `parity` of the barrier to complete, at most timeout_ns
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long timeout_ns)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    for (unsigned int it = 1;; ++it) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((it & 15u) == 0 && (long long)(global_ns() - t0) > timeout_ns) return false;
+    }
+}
+
+// global -> shared bulk copy; dst, src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// order this thread's generic shared-memory accesses before later
+// async-proxy (bulk copy) writes to the same memory
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// shared -> global bulk copy (bulk-group completion); 16-byte aligned, size a
+// multiple of 16
+__device__ __forceinline__ void bulk_store(void* dst, const void* src, uint32_t bytes)
+{
+    asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(dst), "r"(smem_addr(src)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the shared-memory sources of all committed bulk stores have been read
+__device__ __forceinline__ void bulk_wait_read() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// all committed bulk stores have completed
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
+// arrays staged per batch: inputs (NC), then g11 g12 g22 (not for the mass
+// operator), mass (not for Laplace), potential (Helmholtz, Res, f)
+template <int OP>
+__host__ __device__ constexpr int bulk_arrays()
+{
+    return op_nc<OP>() + (OP == OP_MASS ? 0 : 3) + (OP == OP_LAPLACE ? 0 : 1) +
+           ((OP == OP_HELM || OP == OP_RES || OP == OP_F) ? 1 : 0);
+}
+
+template <typename T>
+__host__ __device__ constexpr int bulk_tpb()
+{
+    return sizeof(T) == 4 ? 256 : 128;
+}
+
+constexpr int BULK_STAGES = 2;
+constexpr size_t BULK_SMEM_TARGET = 200 * 1024;
+
+// elements per batch: one line thread per element column (K N <= threads),
+// two stages of every staged array plus two work planes per component within
+// BULK_SMEM_TARGET; a multiple of 4 (FP32) or 2 (FP64) so that a batch of
+// any field is a multiple of 16 bytes
+template <typename T, int OP>
+__host__ __device__ constexpr int bulk_k(int N)
+{
+    const int q = sizeof(T) == 4 ? 4 : 2;
+    const int by_lines = bulk_tpb<T>() / N;
+    const int per_node = (BULK_STAGES * bulk_arrays<OP>() + 2 * op_nc<OP>()) * (int)sizeof(T);
+    const int by_smem = (int)(BULK_SMEM_TARGET / (size_t)(per_node * N * N));
+    const int k = (by_lines < by_smem ? by_lines : by_smem) / q * q;
+    return k < q ? q : k;
+}
+
+template <int N, typename T, int OP>
+__host__ __device__ constexpr size_t bulk_smem_bytes()
+{
+    return 128 + (size_t)(BULK_STAGES * bulk_arrays<OP>() + 2 * op_nc<OP>()) * bulk_k<T, OP>(N) * N * N * sizeof(T);
+}
+
+// D(i,k) at [i*N+k], passed by value: the kernel reads it from the constant
+// bank as an operand of its FMAs
+template <int N, typename T>
+struct DMat {
+    T d[N * N];
+};
+
+// One batch = K elements.  After the stage of a batch has arrived (and, for
+// masked inputs, its non-owner ring copies are patched), thread
+// t = le*N + l works on line l of element le:
+//   P1  column l: ur(:,l) = D u(:,l) (kept in registers);
+//       row l:    us(l,:) = u(l,:) D^T          -> W1
+//   P2  column l: f1 = g11 ur - g12 us, f2 = g22 us - g12 ur; f2 -> W1,
+//       lap1(:,l) = D^T f1(:,l)                 -> W2
+//   P3  row l:    lap(l,:) = lap1(l,:) + f2(l,:) D, then the mass/potential
+//       epilogue of the operator                -> W2
+// and W2 is written out with one bulk store per component.  Every
+// accumulation runs over k in ascending order as in apply_range, so both
+// kernels give the same bits.
+template <int N, typename T, int OP, bool GATHER>
+__global__ void __launch_bounds__(bulk_tpb<T>())
+    k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
+                 const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk,
+                 long long timeout_ns)
+{
+    constexpr int NN = N * N;
+    constexpr int NC = op_nc<OP>();
+    constexpr int NA = bulk_arrays<OP>();
+    constexpr int K = bulk_k<T, OP>(N);
+    constexpr int BN = K * NN;
+    constexpr int S = BULK_STAGES;
+    extern __shared__ __align__(128) unsigned char smb[];
+    uint64_t* bar = (uint64_t*)smb;
+    T* stage0 = (T*)(smb + 128);
+    T* W1 = stage0 + (size_t)S * NA * BN;
+    T* W2 = W1 + NC * BN;
+    const Fac<T> fac = fac_of<T>(m);
+    const T* arr[7];
+    {
+        int a = 0;
+        arr[a++] = in0;
+        if (NC == 2) arr[a++] = in1;
+        if (OP != OP_MASS) {
+            arr[a++] = fac.g11;
+            arr[a++] = fac.g12;
+            arr[a++] = fac.g22;
+        }
+        if (OP != OP_LAPLACE) arr[a++] = fac.mass;
+        if (OP == OP_HELM || OP == OP_RES || OP == OP_F) arr[a++] = pot;
+    }
+    T* outp[2] = {y0, y1};
+    constexpr int A_G11 = NC, A_MASS = (OP == OP_MASS) ? NC : NC + 3, A_POT = A_MASS + 1;
+    const long long nfull = m.E / K;  // batches loaded by bulk copies
+    const long long nbatch = (m.E + K - 1) / K;
+    const long long G = gridDim.x;
+    uint32_t pending = 0;  // thread 0: stages with a copy in flight
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    auto issue = [&](long long b, int s) {  // thread 0 only
+        if (b >= nfull) return;
+        T* st = stage0 + (size_t)s * NA * BN;
+        constexpr uint32_t bytes = (uint32_t)(BN * sizeof(T));
+        mbar_arrive_tx(&bar[s], bytes * NA);
+#pragma unroll
+        for (int a = 0; a < NA; ++a) bulk_load(st + a * BN, arr[a] + b * BN, bytes, &bar[s]);
+        pending |= 1u << s;
+    };
+    if (threadIdx.x == 0)
+        for (int s = 0; s < S; ++s) issue(blockIdx.x + s * G, s);
+    int it = 0;
+    for (long long b = blockIdx.x; b < nbatch; b += G, ++it) {
+        const int s = it % S;
+        const uint32_t parity = (uint32_t)((it / S) & 1);
+        T* st = stage0 + (size_t)s * NA * BN;
+        const int e0 = (int)(b * K);
+        const int ne = min(K, m.E - e0);
+        const int total = ne * NN;
+        bool ok = true;
+        if (b < nfull) {
+            ok = mbar_wait(&bar[s], parity, timeout_ns);
+        } else {
+            for (int t = threadIdx.x; t < total; t += blockDim.x)
+#pragma unroll
+                for (int a = 0; a < NA; ++a) st[a * BN + t] = arr[a][(long long)e0 * NN + t];
+        }
+        if (!__syncthreads_and(ok)) {
+            if (threadIdx.x == 0) {
+                atomicExch(m.dev_err, 1);
+                for (int q = 1; q < S; ++q) {  // copies of the other stages still in flight (bounded)
+                    const int sq = (s + q) % S;
+                    if (pending & (1u << sq)) mbar_wait(&bar[sq], (uint32_t)(((it + q) / S) & 1), timeout_ns);
+                }
+                bulk_wait_all();
+            }
+            __syncthreads();
+            return;
+        }
+        if (threadIdx.x == 0) pending &= ~(1u << s);
+        if (GATHER) {
+            // masked input: ring copies that are not the owner take the owner's
+            // value (ring_src); four independent table/value loads per thread
+            constexpr int R = 4 * (N - 1);
+            const int nr = ne * R;
+            const int* rs = m.ring_src + (long long)e0 * R;
+            for (int t0 = threadIdx.x; t0 < nr; t0 += 4 * (int)blockDim.x) {
+                int src[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int t = t0 + q * (int)blockDim.x;
+                    src[q] = t < nr ? __ldg(rs + t) : -1;
+                }
+                T val[4][NC];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (src[q] >= 0) {
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) val[q][c] = arr[c][src[q]];
+                    }
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (src[q] < 0) continue;
+                    const int t = t0 + q * (int)blockDim.x;
+                    const int le = t / R;
+                    const int r = t - le * R;
+                    int ii, jj;
+                    if (r < N - 1) {
+                        ii = r;
+                        jj = 0;
+                    } else if (r < 2 * (N - 1)) {
+                        ii = N - 1;
+                        jj = r - (N - 1);
+                    } else if (r < 3 * (N - 1)) {
+                        ii = N - 1 - (r - 2 * (N - 1));
+                        jj = N - 1;
+                    } else {
+                        ii = 0;
+                        jj = N - 1 - (r - 3 * (N - 1));
+                    }
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) st[c * BN + le * NN + ii + jj * N] = val[q][c];
+                }
+            }
+            __syncthreads();
+        }
+        if (OP == OP_MASS) {
+            for (int t = threadIdx.x; t < total; t += blockDim.x) y0[(long long)e0 * NN + t] = st[A_MASS * BN + t] * st[t];
+        } else {
+            // large elements keep ur in W2 and the components' laplacians in
+            // W2 between uses instead of in registers
+            constexpr bool LOWREG = N * NC * sizeof(T) > 128;
+            const int line = threadIdx.x;
+            const bool act = line < ne * N;
+            const int le = line / N, l = line - (line / N) * N;
+            const int base = le * NN;
+            T ur[LOWREG ? 1 : NC][N];
+            if (LOWREG) {  // W2 is written in P1
+                if (threadIdx.x == 0 && store_bulk) bulk_wait_read();
+                __syncthreads();
+            }
+            // ---- P1
+            if (act) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    const T* uc = st + c * BN + base;
+                    T* urc = ur[LOWREG ? 0 : c];
+                    T v[N], acc[N];
+#pragma unroll
+                    for (int i = 0; i < N; ++i) {
+                        v[i] = uc[l * N + i];
+                        urc[i] = T(0);
+                    }
+#pragma unroll
+                    for (int k = 0; k < N; ++k)
+#pragma unroll
+                        for (int i = 0; i < N; ++i) urc[i] = fma(D.d[i * N + k], v[k], urc[i]);
+                    if (LOWREG) {
+#pragma unroll
+                        for (int i = 0; i < N; ++i) W2[c * BN + base + l * N + i] = urc[i];
+                    }
+#pragma unroll
+                    for (int j = 0; j < N; ++j) {
+                        v[j] = uc[j * N + l];
+                        acc[j] = T(0);
+                    }
+#pragma unroll
+                    for (int k = 0; k < N; ++k)
+#pragma unroll
+                        for (int j = 0; j < N; ++j) acc[j] = fma(D.d[j * N + k], v[k], acc[j]);
+#pragma unroll
+                    for (int j = 0; j < N; ++j) W1[c * BN + base + j * N + l] = acc[j];
+                }
+            }
+            if (!LOWREG && threadIdx.x == 0 && store_bulk) bulk_wait_read();  // W2 of the previous batch read out
+            __syncthreads();
+            // ---- P2
+            if (act) {
+                T g11[N], g12[N], g22[N];
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    g11[i] = st[A_G11 * BN + base + l * N + i];
+                    g12[i] = st[(A_G11 + 1) * BN + base + l * N + i];
+                    g22[i] = st[(A_G11 + 2) * BN + base + l * N + i];
+                }
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    T f1[N], acc[N];
+#pragma unroll
+                    for (int i = 0; i < N; ++i) {
+                        const T us = W1[c * BN + base + l * N + i];
+                        const T urv = LOWREG ? W2[c * BN + base + l * N + i] : ur[LOWREG ? 0 : c][i];
+                        f1[i] = g11[i] * urv - g12[i] * us;
+                        W1[c * BN + base + l * N + i] = g22[i] * us - g12[i] * urv;
+                        acc[i] = T(0);
+                    }
+#pragma unroll
+                    for (int k = 0; k < N; ++k)
+#pragma unroll
+                        for (int i = 0; i < N; ++i) acc[i] = fma(D.d[k * N + i], f1[k], acc[i]);
+#pragma unroll
+                    for (int i = 0; i < N; ++i) W2[c * BN + base + l * N + i] = acc[i];
+                }
+            }
+            __syncthreads();
+            // ---- P3: row l, all components (the Res/f epilogue mixes them)
+            if (act) {
+                T lapr[LOWREG ? 1 : NC][N];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) {
+                    T f2[N];
+                    T* lc = lapr[LOWREG ? 0 : c];
+#pragma unroll
+                    for (int j = 0; j < N; ++j) {
+                        lc[j] = W2[c * BN + base + j * N + l];
+                        f2[j] = W1[c * BN + base + j * N + l];
+                    }
+#pragma unroll
+                    for (int k = 0; k < N; ++k)
+#pragma unroll
+                        for (int j = 0; j < N; ++j) lc[j] = fma(D.d[k * N + j], f2[k], lc[j]);
+                    if (LOWREG) {
+#pragma unroll
+                        for (int j = 0; j < N; ++j) W2[c * BN + base + j * N + l] = lc[j];
+                    }
+                }
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const int q = base + j * N + l;
+                    T lap[NC][1];
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) lap[c][0] = LOWREG ? W2[c * BN + q] : lapr[LOWREG ? 0 : c][j];
+                    T o[NC];
+                    if (OP == OP_LAPLACE) {
+                        o[0] = lap[0][0];
+                    } else {
+                        const T ms = st[A_MASS * BN + q];
+                        const T pv = (OP == OP_HELM || OP == OP_RES || OP == OP_F) ? st[A_POT * BN + q] : T(0);
+                        T u[NC];
+#pragma unroll
+                        for (int c = 0; c < NC; ++c) u[c] = st[c * BN + q];
+                        if (OP == OP_HELM) {
+                            o[0] = lap[0][0] + (ms * pv) * u[0];
+                        } else if (OP == OP_RES) {
+                            const T mv = ms * pv;
+                            const T Lv = lap[NC - 1][0] + mv * u[NC - 1];
+                            const T Lu = lap[0][0] + mv * u[0];
+                            o[0] = ms * u[0] + alpha * Lv;
+                            o[NC - 1] = alpha * Lu - ms * u[NC - 1];
+                        } else {  // OP_F
+                            const T mv = ms * pv;
+                            o[0] = -(lap[NC - 1][0] + mv * u[NC - 1]);
+                            o[NC - 1] = -(lap[0][0] + mv * u[0]);
+                        }
+                    }
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) W2[c * BN + q] = o[c];
+                }
+            }
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (store_bulk && b < nfull) {
+                if (threadIdx.x == 0) {
+#pragma unroll
+                    for (int c = 0; c < NC; ++c)
+                        bulk_store(outp[c] + (long long)e0 * NN, W2 + c * BN, (uint32_t)(BN * sizeof(T)));
+                    bulk_commit();
+                }
+            } else {
+                for (int t = threadIdx.x; t < total; t += blockDim.x)
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) outp[c][(long long)e0 * NN + t] = W2[c * BN + t];
+            }
+        }
+        // stage s free; this thread's shared-memory accesses ordered before
+        // the bulk copy that refills it
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) issue(b + (long long)S * G, s);
+    }
+    if (threadIdx.x == 0) bulk_wait_all();
+}
+
+// grid of k_apply_bulk for one instantiation (occupancy queried once per process)
+template <int N, typename T, int OP, bool GATHER>
+cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
+                                long long timeout_ns, cudaStream_t st)
+{
+    static int blocks_per_sm = -1, sms = 0;
+    constexpr size_t smem = bulk_smem_bytes<N, T, OP>();
+    if (blocks_per_sm < 0) {
+        cudaError_t e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        int dev = 0;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        int nb = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER>, bulk_tpb<T>(),
+                                                                smem)) != cudaSuccess)
+            return e;
+        blocks_per_sm = nb;
+    }
+    if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
+    if (!m.Dh) return cudaErrorInvalidValue;
+    DMat<N, T> D;
+    for (int i = 0; i < N * N; ++i) D.d[i] = (T)m.Dh[i];
+    constexpr int K = bulk_k<T, OP>(N);
+    const long long nbatch = (m.E + K - 1) / K;
+    const int grid = (int)std::min<long long>(nbatch, (long long)sms * blocks_per_sm);
+    const int store_bulk = (((uintptr_t)y0 | (uintptr_t)(y1 ? y1 : y0)) & 15u) == 0;
+    k_apply_bulk<N, T, OP, GATHER>
+        <<<grid, bulk_tpb<T>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, timeout_ns);
+    return cudaGetLastError();
+}
+
+}  // namespace semgb

@@ -201,6 +201,7 @@ struct sem_ctx {
     long long n = 0, dof = 0;
     unsigned flags = 0;
     std::vector<double> x, w, D;           // D column-major
+    std::vector<double> Drow_host;         // D row-major (DevMesh::Dh)
     std::vector<double> coords;            // [n_nodes][2]
     std::vector<int> elements;             // [E][4]
     std::vector<double> J, A, B, C;        // host metrics [E][N][N]
@@ -218,6 +219,7 @@ struct sem_ctx {
     int precond = 0;
     int inner_fused = 1;
     double outer_scale = 1.0;
+    int apply_pipeline = 1;
     // stage-guess history of the SDIRK drivers (persists across calls)
     long long hist_steps = 0;
     int hist_stages = 0;
@@ -474,6 +476,50 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             if (node_bnd[node]) fl[e] |= (4096 << cc);
         }
     for (int k = 0; k < n_nodes; ++k) c->n_bnd_nodes += node_bnd[k];
+    // ring tables of the in-place assembly and the pipelined apply's gather
+    const int R = 4 * (N - 1);
+    std::vector<int> ring_src((size_t)n_el * R, -1), bnd_flat;
+    std::vector<int2> edge_pairs;
+    for (int e = 0; e < n_el; ++e) {
+        for (int r = 0; r < R; ++r) {
+            int ii, jj;
+            if (r < N - 1) {
+                ii = r;
+                jj = 0;
+            } else if (r < 2 * (N - 1)) {
+                ii = N - 1;
+                jj = r - (N - 1);
+            } else if (r < 3 * (N - 1)) {
+                ii = N - 1 - (r - 2 * (N - 1));
+                jj = N - 1;
+            } else {
+                ii = 0;
+                jj = N - 1 - (r - 3 * (N - 1));
+            }
+            const bool ib = (ii == 0 || ii == N - 1), jb = (jj == 0 || jj == N - 1);
+            int src = -1;
+            if (ib && jb) {
+                const int cc = (jj == 0) ? (ii == 0 ? 0 : 1) : (ii == 0 ? 3 : 2);
+                if (!(fl[e] & (256 << cc)) && !(fl[e] & (4096 << cc))) src = csrc[4 * e + cc];
+            } else {
+                const int sd = jb ? (jj == 0 ? 0 : 2) : (ii == N - 1 ? 1 : 3);
+                const int k = jb ? ii : jj;
+                if (!(fl[e] & (1 << sd)) && !(fl[e] & (16 << sd)))
+                    src = (int)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd]);
+            }
+            ring_src[(size_t)e * R + r] = src;
+        }
+        for (int sd = 0; sd < 4; ++sd) {
+            const bool bnd = fl[e] & (16 << sd), own = fl[e] & (1 << sd);
+            for (int k = 1; k < N - 1; ++k) {
+                if (bnd)
+                    bnd_flat.push_back((int)side_pos(e, sd, k));
+                else if (own)
+                    edge_pairs.push_back(
+                        make_int2((int)side_pos(e, sd, k), (int)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd])));
+            }
+        }
+    }
     c->dof = (long long)n_nodes + (long long)c->n_edges * (N - 2) + (long long)n_el * (N - 2) * (N - 2);
 
     // metrics, include/Quad.hpp:39-54 (C as the reference writes it unless corrected)
@@ -583,6 +629,8 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             Drow[i * N + k] = c->D[i + k * N];
             Drowf[i * N + k] = (float)c->D[i + k * N];
         }
+    c->Drow_host = Drow;
+    d.Dh = c->Drow_host.data();
     auto tof = [](const std::vector<double>& v) {
         std::vector<float> f(v.size());
         for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
@@ -599,8 +647,18 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, tof(g22), &d.g22f)) || (s = upload(c, tof(ms), &d.massf)) ||
         (s = upload(c, kdiag, &d.kdiag)) || (s = upload(c, mdiag, &d.mdiag)) ||
         (s = upload(c, fS, &d.fdmS64)) || (s = upload(c, tof(fS), &d.fdmS32)) ||
-        (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)))
+        (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)) ||
+        (s = upload(c, ring_src, &d.ring_src)) || (s = upload(c, edge_pairs, &d.edge_pairs)) ||
+        (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)))
         return s;
+    d.n_pairs = (long long)edge_pairs.size();
+    d.n_bnd = (long long)bnd_flat.size();
+    {
+        void* p = nullptr;
+        if ((s = ctx_alloc(c, &p, sizeof(int)))) return s;
+        SEM_CUDA(cudaMemset(p, 0, sizeof(int)));
+        d.dev_err = (int*)p;
+    }
     SEM_CUDA(cudaMallocHost((void**)&c->h_out, sizeof(SolveOut)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_sync, sizeof(GridSync)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_part, sizeof(double) * 152 * 64));
@@ -742,6 +800,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
             if (!(v > 0 && v <= 1)) return fail(SEM_ERR_ARG, "refinement tolerance scale must be in (0,1]");
             c->outer_scale = v;
             return SEM_OK;
+        case SEM_OPT_APPLY_PIPELINE:
+            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
+            c->apply_pipeline = (int)v;
+            return SEM_OK;
         case SEM_OPT_INNER_ITERATION:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "inner iteration must be 0 or 1");
             c->inner_fused = (int)v;
@@ -852,6 +914,24 @@ extern "C" int sem_global_sum(sem_ctx* c, double* a)
     return SEM_OK;
 }
 
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+// the flag a pipelined apply sets when one of its bounded waits expired;
+// reported (and cleared) at the next synchronising call
+static int check_dev_err(sem_ctx* c)
+{
+    int h = 0;
+    SEM_CUDA(cudaMemcpyAsync(&h, c->dm.dev_err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    if (h) {
+        SEM_CUDA(cudaMemsetAsync(c->dm.dev_err, 0, sizeof(int), c->stream));
+        return fail(SEM_ERR_DEVICE_WAIT, "a bulk-copy wait of an operator apply timed out");
+    }
+    return SEM_OK;
+}
+
+static long long timeout_ns(const sem_ctx* c) { return (long long)(c->timeout_ms * 1e6); }
+
 static int dot_dev(sem_ctx* c, const double* a, const double* b, double* result)
 {
     double* part = nullptr;
@@ -873,7 +953,8 @@ extern "C" int sem_dot(sem_ctx* c, const double* a, const double* b, double* res
 {
     SEM_CHECK_CTX(c);
     if (!a || !b || !result) return fail(SEM_ERR_ARG, "null argument");
-    return dot_dev(c, a, b, result);
+    const int s = dot_dev(c, a, b, result);
+    return s ? s : check_dev_err(c);
 }
 
 extern "C" int sem_vec_axpby(sem_ctx* c, long long n, double a, const double* x, double b,
@@ -917,6 +998,7 @@ static int apply_galerkin(sem_ctx* c, int op, const double* pot, double alpha, c
 {
     const int nc = (op == OP_RES || op == OP_F) ? 2 : 1;
     if (scale == 1.0 && apply_direct(c, sizeof(double), pot, in0, in1, out0, nc == 2 ? out1 : nullptr)) {
+        // FP64: the one-pass kernel (FP64-pipe bound, not memory bound)
         SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
             return launch_apply<decltype(nv)::value>(c->dm, op, false, pot, alpha, in0, in1, out0, out1, true,
                                                      c->stream);
@@ -989,9 +1071,17 @@ extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, 
     SEM_CHECK_CTX(c);
     if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
     if (apply_direct(c, sizeof(float), V, qr, qi, yr, yi)) {
-        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
-            return launch_apply<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true, c->stream);
-        }));
+        if (c->apply_pipeline && aligned16(V) && aligned16(qr) && aligned16(qi)) {
+            SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+                return launch_apply_bulk<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true,
+                                                              timeout_ns(c), c->stream);
+            }));
+        } else {
+            SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+                return launch_apply<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true,
+                                                         c->stream);
+            }));
+        }
         SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
             return launch_ring<decltype(nv)::value>(c->dm, true, DSS_MASK, yr, yi, c->stream);
         }));
@@ -1041,6 +1131,8 @@ static int finish_solve(sem_ctx* c, SolveOut* out, GridSync* sync, sem_solver_re
     SEM_CUDA(cudaMemcpyAsync(c->h_sync, sync, sizeof(GridSync), cudaMemcpyDeviceToHost, c->stream));
     SEM_CUDA(cudaStreamSynchronize(c->stream));
     if (c->h_sync->err) return fail(SEM_ERR_DEVICE_WAIT, "a grid barrier timed out");
+    int s = check_dev_err(c);
+    if (s) return s;
     if (c->profile) {
         float ms = 0.f;
         SEM_CUDA(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
@@ -1342,7 +1434,7 @@ static int schro_publish(SchroRun* r)
     SEM_CUDA(cudaMemcpyAsync(r->psi_re, r->P[r->cur], sizeof(double) * c->n, k, c->stream));
     SEM_CUDA(cudaMemcpyAsync(r->psi_im, r->P[r->cur] + c->n, sizeof(double) * c->n, k, c->stream));
     SEM_CUDA(cudaStreamSynchronize(c->stream));
-    return SEM_OK;
+    return check_dev_err(c);
 }
 
 // b = dt * f(p + sum a_l z_l), masked (schrodinger.hpp:221,229,378,386)
@@ -1411,9 +1503,10 @@ static int norm2_planes(sem_ctx* c, const double* r, double* out)
 
 // Build the per-element features of the extrapolated guess z (its scaled
 // residual, alpha V, mass / alpha); with `use`, let the network predict a
-// correction and keep it only if its FP64 residual is smaller than the
-// extrapolation's (the extrapolation stays the fallback).  *zext receives a
-// copy of the extrapolated guess (the base the targets are measured from).
+// correction and move z along it by the residual-minimising step (none when
+// no positive step lowers the FP64 residual: the extrapolation stays the
+// fallback).  *zext receives a copy of the extrapolated guess (the base the
+// training targets are measured from).
 static int learned_guess(sem_ctx* c, const double* V, double alpha, const double* b, double* z, bool use,
                          double** zext)
 {
@@ -1452,14 +1545,27 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     k.zo = zl;
     if ((s = launch_learn_op(c, k))) return s;
     if ((s = guess_residual(c, V, alpha, b, zl, r2))) return s;
-    double n_ext = 0, n_l = 0;
-    if ((s = norm2_planes(c, r, &n_ext)) || (s = norm2_planes(c, r2, &n_l))) return s;
+    // minimal residual along the predicted correction d = z_l - z_ext:
+    // r(theta) = r_ext - theta A d with A d = r_ext - r_l, so
+    // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|
+    double n_ext = 0, n_l = 0, x1 = 0, x2 = 0;
+    if ((s = norm2_planes(c, r, &n_ext)) || (s = norm2_planes(c, r2, &n_l)) || (s = dot_dev(c, r, r2, &x1)) ||
+        (s = dot_dev(c, r + c->n, r2 + c->n, &x2)))
+        return s;
+    const double rx = x1 + x2;
+    const double den = n_ext - 2.0 * rx + n_l;
+    const double theta = den > 0 ? (n_ext - rx) / den : 0.0;
     c->stats.learned_guesses++;
-    if (n_l < n_ext) {
-        SEM_CUDA(cudaMemcpyAsync(z, zl, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    double ratio = 1.0;
+    if (theta > 0 && n_ext > 0) {
+        k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, 1.0 - theta, zx, theta, zl, z);
+        c->stats.kernel_launches++;
+        SEM_CUDA(cudaGetLastError());
         c->stats.learned_accepted++;
+        ratio = std::sqrt(std::max(0.0, n_ext - (n_ext - rx) * (n_ext - rx) / den) / n_ext);
     }
-    c->stats.last_guess_residual_ratio = n_ext > 0 ? std::sqrt(std::min(n_l, n_ext) / n_ext) : 1.0;
+    c->stats.last_guess_residual_ratio = ratio;
+    c->stats.last_guess_theta = theta;
     return SEM_OK;
 }
 

@@ -61,6 +61,19 @@ struct DevMesh {
     const double* fdmL64 = nullptr;
     const float* fdmL32 = nullptr;
     const float4* fdm_el = nullptr;
+    // ring tables: ring_src[e*4(N-1) + r] = flat index of the owner copy for
+    // the non-owner, non-boundary ring copy r of element e (ring order: j=0
+    // side, i=N-1 side, j=N-1 side reversed, i=0 side reversed), else -1;
+    // edge_pairs = (owner, other) copies of every interior-side node (corners
+    // excluded); bnd_flat = copies on boundary sides (corners excluded);
+    // node_bnd = corner node on the boundary
+    const int* ring_src = nullptr;
+    const int2* edge_pairs = nullptr;
+    const int* bnd_flat = nullptr;
+    const char* node_bnd = nullptr;
+    long long n_pairs = 0, n_bnd = 0;
+    int* dev_err = nullptr;  // set by a kernel whose bounded wait expired (pipelined apply)
+    const double* Dh = nullptr;  // host copy of D, row-major (launchers that pass D by value)
 };
 
 // Grid barrier and error state of a persistent (cooperative) kernel.
@@ -132,6 +145,12 @@ template <int N>
 cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, double alpha,
                          const void* in0, const void* in1, void* y0, void* y1, bool gather,
                          cudaStream_t st);
+// the same operators through the bulk-copy pipeline (k_apply_bulk); every
+// field pointer 16-byte aligned.  FP64: all operators; FP32: Res.
+template <int N>
+cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
+                              const void* in1, void* y0, void* y1, bool gather, long long timeout_ns,
+                              cudaStream_t st);
 template <int N>
 cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
                        void* out, cudaStream_t st);

@@ -5,6 +5,9 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "sem_apply_bulk.cuh"
 #include "sem_device.cuh"
 #include "sem_solvers.cuh"
 
@@ -49,62 +52,42 @@ __global__ void k_dss(DevMesh m, const T* __restrict__ Y, T* __restrict__ out, T
 }
 
 // In-place assembly of element-local values (the apply's own output) that
-// touches only the element rings.  Work items: every (element, side, k) for
-// k = 1..N-2, handled by the side's owner (interior sides) or its element
-// (boundary sides), then every corner node.  One item owns all copies of
-// its global node, so no two threads write the same copy.  Sums run in the
-// order dss_value uses (owner + other on sides; 0 + copies in
-// connected_elements order at corners), so the result equals
-// k_dss<MODE> with scale 1 bit for bit.  Element interiors are final as the
-// apply wrote them.
+// touches only the element rings, from precomputed tables: every
+// interior-side node pair (owner, other), every boundary-side copy, then
+// every corner node over its copies.  One item owns all copies of its
+// global node, so no two threads write the same copy.  Sums run in the order
+// dss_value uses (owner + other on sides; 0 + copies in connected_elements
+// order at corners), so the result equals k_dss<MODE> with scale 1 bit for
+// bit.  Element interiors are final as the apply wrote them.
 template <int N, typename T, int MODE>
 __global__ void k_ring(DevMesh m, T* __restrict__ a0, T* __restrict__ a1)
 {
-    constexpr int NN = N * N;
-    constexpr int NS = N - 2;  // interior nodes per side
-    constexpr int NSd = NS > 0 ? NS : 1;
-    const long long n_side = (long long)m.E * 4 * NS;
-    const long long total = n_side + m.n_nodes;
+    const long long np = m.n_pairs, nb = m.n_bnd;
+    const long long total = np + nb + m.n_nodes;
+    T* planes[2] = {a0, a1};
     for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
          it += (long long)gridDim.x * blockDim.x) {
-        if (it < n_side) {
-            const int e = (int)(it / (4 * NSd));
-            const int r = (int)(it - (long long)e * 4 * NSd);
-            const int sd = r / NSd, k = 1 + r % NSd;
-            const int fl = __ldg(m.flags + e);
-            const bool bnd = (fl >> (4 + sd)) & 1;
-            if (!bnd && !((fl >> sd) & 1)) continue;  // the neighbour owns this side
-            const int i = sd == 0 ? k : sd == 1 ? N - 1 : sd == 2 ? k : 0;
-            const int j = sd == 0 ? 0 : sd == 1 ? k : sd == 2 ? N - 1 : k;
-            const long long o = (long long)e * NN + j * N + i;
-            if (bnd) {
-                if (MODE != DSS_SUM) {
-                    a0[o] = T(0);
-                    if (a1) a1[o] = T(0);
-                }
-                continue;
-            }
-            const long long nf = (long long)__ldg(m.side_base + 4 * e + sd) + (long long)k * __ldg(m.side_step + 4 * e + sd);
-            T* planes[2] = {a0, a1};
+        if (it < np) {
+            const int2 pr = __ldg(m.edge_pairs + it);
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 T* a = planes[q];
                 if (!a) continue;
-                const T v = a[o] + a[nf];
-                a[o] = v;
-                a[nf] = MODE == DSS_MASK ? T(0) : v;
+                const T v = a[pr.x] + a[pr.y];
+                a[pr.x] = v;
+                a[pr.y] = MODE == DSS_MASK ? T(0) : v;
             }
+        } else if (it < np + nb) {
+            if (MODE == DSS_SUM) continue;
+            const int f = __ldg(m.bnd_flat + (it - np));
+#pragma unroll
+            for (int q = 0; q < 2; ++q)
+                if (planes[q]) planes[q][f] = T(0);
         } else {
-            const int node = (int)(it - n_side);
+            const int node = (int)(it - np - nb);
             const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
             if (q1 <= q0) continue;
-            const long long f0 = __ldg(m.node_flat + q0);
-            const int e = (int)(f0 / NN);
-            const int loc = (int)(f0 - (long long)e * NN);
-            const int i = loc % N, j = loc / N;
-            const int c = (j == 0) ? (i == 0 ? 0 : 1) : (i == 0 ? 3 : 2);
-            const bool bnd = (__ldg(m.flags + e) >> (12 + c)) & 1;
-            T* planes[2] = {a0, a1};
+            const bool bnd = __ldg(m.node_bnd + node) != 0;
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 T* a = planes[q];
@@ -373,6 +356,24 @@ cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, d
 }
 
 template <int N>
+cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
+                              const void* in1, void* y0, void* y1, bool gather, long long timeout_ns,
+                              cudaStream_t st)
+{
+#define SEM_BULK_CASE(T, OPK)                                                                                 \
+    return gather ? launch_apply_bulk_t<N, T, OPK, true>(m, (const T*)pot, (T)alpha, (const T*)in0,           \
+                                                         (const T*)in1, (T*)y0, (T*)y1, timeout_ns, st)        \
+                  : launch_apply_bulk_t<N, T, OPK, false>(m, (const T*)pot, (T)alpha, (const T*)in0,          \
+                                                          (const T*)in1, (T*)y0, (T*)y1, timeout_ns, st);
+    if (!fp32) return cudaErrorInvalidValue;  // FP64 applies are FP64-pipe bound: one-pass kernel
+    switch (op) {
+        case OP_RES: SEM_BULK_CASE(float, OP_RES)
+        default: return cudaErrorInvalidValue;
+    }
+#undef SEM_BULK_CASE
+}
+
+template <int N>
 cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
                        void* out, cudaStream_t st)
 {
@@ -443,7 +444,7 @@ template <int N>
 cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, cudaStream_t st)
 {
     const int tpb = 256;
-    const int grid = grid_for((long long)m.E * 4 * (N - 2) + m.n_nodes, tpb);
+    const int grid = grid_for(m.n_pairs + m.n_bnd + m.n_nodes, tpb);
 #define SEM_RING_CASE(T)                                                                                  \
     switch (mode) {                                                                                       \
         case DSS_SUM: k_ring<N, T, DSS_SUM><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;             \
@@ -485,6 +486,9 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
     template cudaError_t launch_dss<NV>(const DevMesh&, bool, int, double, const void*, void*,       \
                                         cudaStream_t);                                               \
     template cudaError_t launch_ring<NV>(const DevMesh&, bool, int, void*, void*, cudaStream_t);     \
+    template cudaError_t launch_apply_bulk<NV>(const DevMesh&, int, bool, const void*, double,       \
+                                               const void*, const void*, void*, void*, bool,         \
+                                               long long, cudaStream_t);                             \
     template cudaError_t launch_unmask<NV>(const DevMesh&, bool, void*, cudaStream_t);               \
     template cudaError_t launch_mask<NV>(const DevMesh&, bool, void*, cudaStream_t);                 \
     template cudaError_t launch_dot<NV>(const DevMesh&, const double*, const double*, double*, int,  \

@@ -25,6 +25,8 @@ def main():
     ap.add_argument("--prec", default="fp64", choices=["fp64", "fp32", "mixed"])
     ap.add_argument("--tol", type=float, default=1e-10, help="0 runs exactly maxit iterations")
     ap.add_argument("--time", action="store_true", help="print device time per iteration")
+    ap.add_argument("--pipeline", type=int, default=1, help="apply: 1 bulk-copy pipelined kernel, 0 one-pass")
+    ap.add_argument("--precond", type=int, default=0, help="mixed minres: 0 none, 1 diagonal, 2 element FDM")
     a = ap.parse_args()
     import torch
 
@@ -38,6 +40,7 @@ def main():
     re, im = gaussian_packet(X, Y, (-2.0, 0.0), 1.0, (3.0, 0.0))
     V = X * X + Y * Y
     if a.case == "apply":
+        ctx.set_option(capi.OPT_APPLY_PIPELINE, a.pipeline)
         dt = torch.float64 if a.prec == "fp64" else torch.float32
         q = [ctx.to_device(t, dt) for t in (re, im, V)]
         f = ctx.schro_res if a.prec == "fp64" else ctx.schro_res_f32
@@ -49,6 +52,7 @@ def main():
         ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
         ctx.set_option(capi.OPT_INNER_TOL, max(a.tol, 1e-30))
         ctx.set_option(capi.OPT_MAX_REFINE, 1)
+        ctx.set_option(capi.OPT_PRECOND, a.precond)
     ctx.set_option(capi.OPT_PROFILE, 1)
     dV = ctx.to_device(V)
     br, bi = ctx.schro_f(dV, ctx.to_device(re), ctx.to_device(im))

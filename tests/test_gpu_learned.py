@@ -134,6 +134,8 @@ def test_learned_stage_guess_in_driver(semlib, torch_mod):
     a_re, a_im = packet(*test_pk)
     assert ctx.schrodinger("dirk4s3", a_re, a_im, V, (steps - 0.5) * dt, dt, maxit, tol)
     ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    ctx.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
+    ctx.set_option(capi.OPT_REFINE_TOL_SCALE, 0.1)
     ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_EXTRAPOLATE)
     train = [((-2.0, 1.0), 1.0, (2.0, 1.0)), ((1.0, -1.0), 0.7, (-3.0, 2.0)), ((0.5, 1.5), 1.2, (1.0, -3.0))]
     n_train = 8
@@ -164,8 +166,12 @@ def test_learned_stage_guess_in_driver(semlib, torch_mod):
     s1 = ctx.stats()
     assert s1.learned_guesses - s0.learned_guesses == 3 * (steps - 2)
     assert s1.learned_accepted > s0.learned_accepted
-    print("extrapolated", its[capi.GUESS_EXTRAPOLATE], "learned", its[capi.GUESS_LEARNED],
-          "accepted", s1.learned_accepted - s0.learned_accepted)
+    assert 0.0 <= s1.last_guess_residual_ratio <= 1.0
+    ext, lrn = its[capi.GUESS_EXTRAPOLATE], its[capi.GUESS_LEARNED]
+    print("extrapolated", ext, "learned", lrn, "accepted", s1.learned_accepted - s0.learned_accepted,
+          "last ratio", s1.last_guess_residual_ratio, "theta", s1.last_guess_theta)
+    # what the network gains over the extrapolation alone (steps 3.., where it runs)
+    assert sum(lrn[2:]) < sum(ext[2:])
 
 
 def test_set_learner_checks_shape(semlib):
