@@ -74,6 +74,9 @@ enum sem_option {
                                     recurrence), 0 the two-barrier form of the FP64 solver */
     SEM_OPT_REFINE_TOL_SCALE = 9, /* mixed mode stops at |r| < s (tol |r0| + tol), s in (0,1],
                                     default 1 (the reference's test on the true residual) */
+    SEM_OPT_EXTRAP_ORDER = 11,   /* stage guess of SEM_GUESS_EXTRAPOLATE / _LEARNED: 1 (default)
+                                    linear 2 z1 - z2, 2 quadratic 3 z1 - 3 z2 + z3 once three
+                                    previous steps exist */
     SEM_OPT_APPLY_PIPELINE = 10  /* FP32 standalone apply: 1 (default) bulk-copy pipelined element
                                     kernel when the input fields are 16-byte aligned, 0 the
                                     one-pass kernel; same results bit for bit.  A pipelined
@@ -307,6 +310,49 @@ int sem_ctx_record(sem_ctx* ctx, long long capacity_rows);
 /* the recorded dataset: device pointers X (BF16 rows x d_in), T (FP32 rows x
  * d_out), rows recorded, d_in = 4 N^2, d_out = 2 N^2 */
 int sem_ctx_dataset(sem_ctx* ctx, void** X, float** T, long long* rows, int* d_in, int* d_out);
+
+/* ------------------------------------------------- batched ensembles (device)
+ * No counterpart in the reference (its drivers step one mesh).  Many
+ * independent instances -- each with its own mesh (p = 2..8), potential and
+ * state -- advanced together by schro_omp::schrodinger_bdf2
+ * (include/openmp_impl/schrodinger.hpp:22-128) with the mixed-precision
+ * stage solve (FP32 inner MINRES, FP64 refinement on the true residual;
+ * SEM_PRECOND_FDM by default).  One persistent launch per time step serves
+ * all instances (a block per instance, largest first, block-local barriers
+ * and reductions); the step is captured once as a CUDA graph and replayed.
+ * The elements each block stages per pass are chosen per degree by a timing
+ * sweep at creation (sem_batch_stats.kmax_of_p). */
+typedef struct sem_batch sem_batch;
+typedef struct {
+    long long steps;              /* time steps run (all instances together) */
+    long long instance_steps;     /* instance-steps */
+    long long krylov_iterations;  /* FP32 inner iterations over all instances */
+    long long graph_launches;     /* replays of the captured step */
+    long long graphs_built;       /* step captures */
+    double kernel_ms;             /* device time of the replayed steps */
+    int kmax_of_p[17];            /* elements staged per pass, by degree p (0: absent) */
+} sem_batch_stats;
+/* instance i: degree p[i], n_nodes[i] corner coordinates coords[i] (x,y
+ * pairs), n_elements[i] quads elements[i] (4 counter-clockwise corner ids) */
+int sem_batch_create(sem_batch** batch, int n_instances, const int* p, const int* n_nodes,
+                     const double* const* coords, const int* n_elements, const int* const* elements,
+                     unsigned flags);
+int sem_batch_destroy(sem_batch* batch);
+int sem_batch_set_stream(sem_batch* batch, void* cuda_stream);
+/* SEM_OPT_INNER_TOL, SEM_OPT_MAX_REFINE, SEM_OPT_REFINE_TOL_SCALE,
+ * SEM_OPT_PRECOND (NONE or FDM); SEM_OPT_SOLVE_PRECISION only MIXED */
+int sem_batch_set_option(sem_batch* batch, int option, double value);
+int sem_batch_get_info(const sem_batch* batch, int instance, sem_mesh_info* info);
+int sem_batch_get_stats(const sem_batch* batch, sem_batch_stats* stats);
+/* after a driver call: steps taken, whether the instance stopped on a failed
+ * solve, and its inner iterations */
+int sem_batch_get_instance(const sem_batch* batch, int instance, int* steps, int* stopped,
+                           long long* iterations);
+/* schrodinger_bdf2 for every instance at once: per-instance field pointers
+ * (host or device), in/out state; success[i] as the reference's return */
+int sem_batch_schrodinger_bdf2(sem_batch* batch, double* const* psi_re, double* const* psi_im,
+                               const double* const* V, double T, const sem_solver_opts* opts,
+                               int* success);
 
 #ifdef __cplusplus
 }

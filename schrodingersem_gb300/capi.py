@@ -42,6 +42,12 @@ class SemStats(C.Structure):
                 ("last_guess_theta", C.c_double)]
 
 
+class SemBatchStats(C.Structure):
+    _fields_ = [("steps", C.c_longlong), ("instance_steps", C.c_longlong), ("krylov_iterations", C.c_longlong),
+                ("graph_launches", C.c_longlong), ("graphs_built", C.c_longlong), ("kernel_ms", C.c_double),
+                ("kmax_of_p", C.c_int * 17)]
+
+
 STEP_CALLBACK = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, _dp, _dp)
 
 # name -> (restype, argtypes); every function declared in include/sem_gb300.h
@@ -96,6 +102,17 @@ SIGNATURES = {
     "sem_learner_fit": (C.c_int, [_vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _dp]),
     "sem_gemm_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
     "sem_ctx_set_learner": (C.c_int, [_vp, _vp]),
+    "sem_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                   C.POINTER(_vp), C.POINTER(C.c_int), C.POINTER(_vp), C.c_uint]),
+    "sem_batch_destroy": (C.c_int, [_vp]),
+    "sem_batch_set_stream": (C.c_int, [_vp, _vp]),
+    "sem_batch_set_option": (C.c_int, [_vp, C.c_int, C.c_double]),
+    "sem_batch_get_info": (C.c_int, [_vp, C.c_int, C.POINTER(SemMeshInfo)]),
+    "sem_batch_get_stats": (C.c_int, [_vp, C.POINTER(SemBatchStats)]),
+    "sem_batch_get_instance": (C.c_int, [_vp, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                         C.POINTER(C.c_longlong)]),
+    "sem_batch_schrodinger_bdf2": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.c_double,
+                                             C.POINTER(SemSolverOpts), C.POINTER(C.c_int)]),
     "sem_ctx_record": (C.c_int, [_vp, C.c_longlong]),
     "sem_ctx_dataset": (C.c_int, [_vp, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(C.c_longlong),
                                   C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -103,7 +120,7 @@ SIGNATURES = {
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
-OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE = 7, 8, 9, 10
+OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_EXTRAP_ORDER = 7, 8, 9, 10, 11
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

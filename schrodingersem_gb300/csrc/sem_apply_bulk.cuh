@@ -114,12 +114,12 @@ __host__ __device__ constexpr int bulk_tpb()
     return sizeof(T) == 4 ? 256 : 128;
 }
 
-constexpr int BULK_STAGES = 2;
+constexpr int BULK_STAGES = 2;  // one batch in flight while one computes (3 measured slower)
 constexpr size_t BULK_SMEM_TARGET = 200 * 1024;
 
 // elements per batch: one line thread per element column (K N <= threads),
-// two stages of every staged array plus two work planes per component within
-// BULK_SMEM_TARGET; a multiple of 4 (FP32) or 2 (FP64) so that a batch of
+// BULK_STAGES stages of every staged array plus two work planes per
+// component within BULK_SMEM_TARGET; a multiple of 4 (FP32) or 2 (FP64) so that a batch of
 // any field is a multiple of 16 bytes
 template <typename T, int OP>
 __host__ __device__ constexpr int bulk_k(int N)
@@ -210,6 +210,56 @@ __global__ void __launch_bounds__(bulk_tpb<T>())
     };
     if (threadIdx.x == 0)
         for (int s = 0; s < S; ++s) issue(blockIdx.x + s * G, s);
+    // masked input: ring copies that are not the owner take the owner's value
+    // (ring_src).  The table entries and values of a block's next batch are
+    // loaded into registers while the current batch computes.
+    constexpr int R = 4 * (N - 1);
+    constexpr int TPB = bulk_tpb<T>();
+    constexpr int GQ = (K * R + TPB - 1) / TPB;
+    int gsrc[GQ];
+    T gval[GQ][NC];
+    auto gather_fetch = [&](long long bb) {
+        const int neb = bb < nbatch ? min(K, m.E - (int)(bb * K)) : 0;
+        const int nr = neb * R;
+        const int* rs = m.ring_src + bb * K * R;
+#pragma unroll
+        for (int q = 0; q < GQ; ++q) {
+            const int t = threadIdx.x + q * TPB;
+            gsrc[q] = t < nr ? __ldg(rs + t) : -1;
+        }
+#pragma unroll
+        for (int q = 0; q < GQ; ++q)
+            if (gsrc[q] >= 0) {
+#pragma unroll
+                for (int c = 0; c < NC; ++c) gval[q][c] = arr[c][gsrc[q]];
+            }
+    };
+    auto gather_apply = [&](T* st, int ne) {
+#pragma unroll
+        for (int q = 0; q < GQ; ++q) {
+            if (gsrc[q] < 0) continue;
+            const int t = threadIdx.x + q * TPB;
+            const int le = t / R;
+            const int r = t - le * R;
+            int ii, jj;
+            if (r < N - 1) {
+                ii = r;
+                jj = 0;
+            } else if (r < 2 * (N - 1)) {
+                ii = N - 1;
+                jj = r - (N - 1);
+            } else if (r < 3 * (N - 1)) {
+                ii = N - 1 - (r - 2 * (N - 1));
+                jj = N - 1;
+            } else {
+                ii = 0;
+                jj = N - 1 - (r - 3 * (N - 1));
+            }
+#pragma unroll
+            for (int c = 0; c < NC; ++c) st[c * BN + le * NN + ii + jj * N] = gval[q][c];
+        }
+    };
+    if (GATHER) gather_fetch(blockIdx.x);
     int it = 0;
     for (long long b = blockIdx.x; b < nbatch; b += G, ++it) {
         const int s = it % S;
@@ -240,50 +290,9 @@ __global__ void __launch_bounds__(bulk_tpb<T>())
         }
         if (threadIdx.x == 0) pending &= ~(1u << s);
         if (GATHER) {
-            // masked input: ring copies that are not the owner take the owner's
-            // value (ring_src); four independent table/value loads per thread
-            constexpr int R = 4 * (N - 1);
-            const int nr = ne * R;
-            const int* rs = m.ring_src + (long long)e0 * R;
-            for (int t0 = threadIdx.x; t0 < nr; t0 += 4 * (int)blockDim.x) {
-                int src[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    const int t = t0 + q * (int)blockDim.x;
-                    src[q] = t < nr ? __ldg(rs + t) : -1;
-                }
-                T val[4][NC];
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    if (src[q] >= 0) {
-#pragma unroll
-                        for (int c = 0; c < NC; ++c) val[q][c] = arr[c][src[q]];
-                    }
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    if (src[q] < 0) continue;
-                    const int t = t0 + q * (int)blockDim.x;
-                    const int le = t / R;
-                    const int r = t - le * R;
-                    int ii, jj;
-                    if (r < N - 1) {
-                        ii = r;
-                        jj = 0;
-                    } else if (r < 2 * (N - 1)) {
-                        ii = N - 1;
-                        jj = r - (N - 1);
-                    } else if (r < 3 * (N - 1)) {
-                        ii = N - 1 - (r - 2 * (N - 1));
-                        jj = N - 1;
-                    } else {
-                        ii = 0;
-                        jj = N - 1 - (r - 3 * (N - 1));
-                    }
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) st[c * BN + le * NN + ii + jj * N] = val[q][c];
-                }
-            }
+            gather_apply(st, ne);
             __syncthreads();
+            gather_fetch(b + G);  // in flight while this batch computes
         }
         if (OP == OP_MASS) {
             for (int t = threadIdx.x; t < total; t += blockDim.x) y0[(long long)e0 * NN + t] = st[A_MASS * BN + t] * st[t];

@@ -569,6 +569,7 @@ __device__ __forceinline__ unsigned long long global_ns()
 __device__ __forceinline__ bool grid_barrier(GridSync* gs, long long timeout_ns)
 {
     __syncthreads();
+    if (!gs) return true;  // block-local solve (batched instances): the block barrier suffices
     if (threadIdx.x == 0) {
         const unsigned int inc = (blockIdx.x == 0) ? (0x80000000u - (gridDim.x - 1)) : 1u;
         volatile unsigned int* vc = &gs->count;

@@ -220,6 +220,7 @@ struct sem_ctx {
     int inner_fused = 1;
     double outer_scale = 1.0;
     int apply_pipeline = 1;
+    int extrap_order = 1;
     // stage-guess history of the SDIRK drivers (persists across calls)
     long long hist_steps = 0;
     int hist_stages = 0;
@@ -799,6 +800,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_REFINE_TOL_SCALE:
             if (!(v > 0 && v <= 1)) return fail(SEM_ERR_ARG, "refinement tolerance scale must be in (0,1]");
             c->outer_scale = v;
+            return SEM_OK;
+        case SEM_OPT_EXTRAP_ORDER:
+            if (v != 1 && v != 2) return fail(SEM_ERR_ARG, "extrapolation order must be 1 or 2");
+            c->extrap_order = (int)v;
             return SEM_OK;
         case SEM_OPT_APPLY_PIPELINE:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
@@ -1673,8 +1678,9 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
         bw = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0, 0.25};
         ew = {-3.0 / 16.0, -27.0 / 32.0, 25.0 / 32.0, 0.0, 0.25};
     }
-    // stage solutions of the current and the two previous steps (ring of 3)
+    // stage solutions of the current and the three previous steps (ring of 4)
     const size_t zset = (size_t)stages * 2 * c->n;
+    constexpr int RING = 4;
     const bool extrap = (c->guess == SEM_GUESS_EXTRAPOLATE || c->guess == SEM_GUESS_LEARNED) &&
                         c->prec == SEM_PREC_MIXED;
     // the stage history carries over from the previous driver call when it
@@ -1697,7 +1703,7 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
     double* Zring = nullptr;
     double* Z = nullptr;
     double* b = nullptr;
-    if ((s = wsget(c, "drv_Z", (extrap ? 3 : 1) * zset, &Zring))) return s;
+    if ((s = wsget(c, "drv_Z", (extrap ? RING : 1) * zset, &Zring))) return s;
     Z = Zring;
     if ((s = wsget(c, "drv_b2", 2 * c->n, &b))) return s;
     double pnorm = 0.0;
@@ -1712,7 +1718,7 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
     while (t < T) {  // schrodinger.hpp:219, 376
         c->stats.last_step_stages = stages;
         const long long gstep = hist0 + step;  // steps of this trajectory so far
-        if (extrap) Z = Zring + (size_t)(gstep % 3) * zset;
+        if (extrap) Z = Zring + (size_t)(gstep % RING) * zset;
         for (int st = 0; st < stages; ++st) {
             ZList zl{};
             zl.nz = st;
@@ -1723,12 +1729,28 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             if ((s = schro_rhs(&r, o->dt, zl, b))) return s;
             double* z = Z + (size_t)st * 2 * c->n;
             // initial guess: zero as the reference (schrodinger.hpp:222,379), or
-            // the stage's solution extrapolated linearly from the last two steps
+            // the stage's solution extrapolated from the previous steps: linear
+            // 2 z1 - z2, or (SEM_OPT_EXTRAP_ORDER 2) quadratic 3 z1 - 3 z2 + z3
             int x_zero = 1;
+            auto hz = [&](long long back) {
+                return Zring + (size_t)((gstep - back) % RING) * zset + (size_t)st * 2 * c->n;
+            };
             if (extrap && gstep >= 1) {
-                const double* z1 = Zring + (size_t)((gstep - 1) % 3) * zset + (size_t)st * 2 * c->n;
-                if (gstep >= 2) {
-                    const double* z2 = Zring + (size_t)((gstep - 2) % 3) * zset + (size_t)st * 2 * c->n;
+                const double* z1 = hz(1);
+                if (gstep >= 3 && c->extrap_order == 2) {
+                    ZList q{};
+                    q.nz = 3;
+                    q.z[0] = z1;
+                    q.c[0] = 3.0;
+                    q.z[1] = hz(2);
+                    q.c[1] = -3.0;
+                    q.z[2] = hz(3);
+                    q.c[2] = 1.0;
+                    k_lincomb<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, q, z);
+                    c->stats.kernel_launches++;
+                    SEM_CUDA(cudaGetLastError());
+                } else if (gstep >= 2) {
+                    const double* z2 = hz(2);
                     k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, 2.0, z1, -1.0, z2, z);
                     c->stats.kernel_launches++;
                     SEM_CUDA(cudaGetLastError());

@@ -65,19 +65,37 @@ __global__ void k_ring(DevMesh m, T* __restrict__ a0, T* __restrict__ a1)
     const long long np = m.n_pairs, nb = m.n_bnd;
     const long long total = np + nb + m.n_nodes;
     T* planes[2] = {a0, a1};
-    for (long long it = blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total;
-         it += (long long)gridDim.x * blockDim.x) {
-        if (it < np) {
-            const int2 pr = __ldg(m.edge_pairs + it);
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    // side pairs, four per thread with their loads issued together
+    for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < np; i0 += 4 * stride) {
+        int2 pr[4];
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                T* a = planes[q];
-                if (!a) continue;
-                const T v = a[pr.x] + a[pr.y];
-                a[pr.x] = v;
-                a[pr.y] = MODE == DSS_MASK ? T(0) : v;
-            }
-        } else if (it < np + nb) {
+        for (int q = 0; q < 4; ++q) {
+            const long long i = i0 + q * stride;
+            pr[q] = i < np ? __ldg(m.edge_pairs + i) : make_int2(-1, -1);
+        }
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+            T* a = planes[c];
+            if (!a) continue;
+            T x[4], y[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (pr[q].x >= 0) {
+                    x[q] = a[pr[q].x];
+                    y[q] = a[pr[q].y];
+                }
+#pragma unroll
+            for (int q = 0; q < 4; ++q)
+                if (pr[q].x >= 0) {
+                    const T v = x[q] + y[q];
+                    a[pr[q].x] = v;
+                    a[pr[q].y] = MODE == DSS_MASK ? T(0) : v;
+                }
+        }
+    }
+    for (long long it = np + blockIdx.x * (long long)blockDim.x + threadIdx.x; it < total; it += stride) {
+        if (it < np + nb) {
             if (MODE == DSS_SUM) continue;
             const int f = __ldg(m.bnd_flat + (it - np));
 #pragma unroll

@@ -55,6 +55,12 @@ __device__ __forceinline__ void grid_sum2_t(T v0, T v1, double* partials, int sl
 {
     const double b0 = block_sum_t<T>(v0, red);
     const double b1 = block_sum_t<T>(v1, red);
+    if (!gs) {  // block-local solve: the block sums are the sums
+        ok = true;
+        r0 = b0;
+        r1 = b1;
+        return;
+    }
     const int G = gridDim.x;
     double* p0 = partials + (size_t)(slot * 2) * G;
     double* p1 = p0 + G;
@@ -681,25 +687,28 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
 // with the true residual in place of the recursive estimate; with rel_to_b,
 // |b| replaces |r_0|); else solve A d = r in FP32 to relative tolerance
 // inner_tol and add d to x in FP64 on owner copies.
-template <int N, int OP>
-__global__ void __launch_bounds__(SOLVER_TPB, 1)
-    k_minres_mixed(DevMesh m, SolveArgs a, KrylovWork<float> w, MixedArgs mx)
+//
+// The refinement itself is a device function over the element range
+// [eb, ee): the cooperative kernel gives every block a slice of one mesh
+// (grid barriers and grid reductions); the batched kernel gives one block a
+// whole instance (a.sync == nullptr: block barriers and block reductions).
+// Returns false when a wait timed out.  `leader` writes a.out.  LEAN
+// compiles only the unpreconditioned and element-preconditioned inner
+// iterations (the batched kernels).
+template <int N, int OP, bool LEAN = false>
+__device__ __forceinline__ bool mixed_solve(const DevMesh& m, const SolveArgs& a, const KrylovWork<float>& w,
+                                            const MixedArgs& mx, int eb, int ee, bool leader,
+                                            unsigned char* smraw, double* red, MinresScal<float>& sc,
+                                            double* sweep_state, float* fdmS, float* fdmL)
 {
     constexpr int NN = N * N;
     constexpr int NC = op_nc<OP>();
-    extern __shared__ __align__(16) unsigned char smraw[];
-    __shared__ double red[34];
-    __shared__ MinresScal<float> sc;
-    __shared__ double sweep_state[3];  // r0, |r|, done
-    __shared__ float fdmS[NN], fdmL[N];  // element preconditioner basis
     double* sm64 = (double*)smraw;
     float* sm32 = (float*)smraw;
     const Fac<double> fac64 = fac_of<double>(m);
     const double* pot64 = (const double*)a.pot;
     const double* bp[2] = {(const double*)a.b[0], (const double*)a.b[1]};
     double* xp[2] = {(double*)a.x[0], (double*)a.x[1]};
-    int eb, ee;
-    block_range(m.E, eb, ee);
     const long long nb = (long long)eb * NN, ne = (long long)ee * NN;
     const int kmax = a.kmax;
     int slot = 0;
@@ -724,7 +733,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
 #pragma unroll
                         for (int c = 0; c < NC; ++c) mx.Y64[c][flat] = o[c];
                     });
-            if (!grid_barrier(a.sync, a.timeout_ns)) return;
+            if (!grid_barrier(a.sync, a.timeout_ns)) return false;
         }
         double part = 0.0, partb = 0.0;
         const bool want_b = (sweep == 0) && a.rel_to_b;
@@ -751,7 +760,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         double rr = 0.0, bbv = 0.0;
         grid_sum2_t<double>(part, partb, w.partials, slot, a.sync, a.timeout_ns, red, ok, rr, bbv);
         slot ^= 1;
-        if (!ok) return;
+        if (!ok) return false;
         if (threadIdx.x == 0) {
             const double rn = sqrt(rr);
             if (sweep == 0) sweep_state[0] = want_b ? sqrt(bbv) : rn;
@@ -784,6 +793,10 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
             }
         }
         if (done_fdm) {
+        } else if constexpr (LEAN) {  // batched instances: no preconditioner or the element one
+            okc = minres_core<N, float, OP, 0>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee, w, a.sync,
+                                               a.timeout_ns, slot, rhs, mx.x32, budget, mx.inner_tol, 0.0, ir,
+                                               (const float*)nullptr);
         } else if (OP == OP_RES && mx.fused)
             okc = mx.pinv32
                       ? minres_core_fused<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb,
@@ -800,7 +813,7 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
                       : minres_core<N, float, OP, 0>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
                                                          w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
                                                          mx.inner_tol, 0.0, ir, (const float*)nullptr);
-        if (!okc) return;
+        if (!okc) return false;
         inner_total += ir.it;
         ++sweep;
         // ---- x += d (FP64, owner copies; d is zero on the others)
@@ -808,9 +821,9 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
 #pragma unroll
             for (int c = 0; c < NC; ++c) xp[c][idx] += (double)mx.x32[c][idx];
         }
-        if (!grid_barrier(a.sync, a.timeout_ns)) return;
+        if (!grid_barrier(a.sync, a.timeout_ns)) return false;
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (leader && threadIdx.x == 0) {
         a.out->success = conv ? 1 : 0;
         a.out->n_iter = inner_total;
         a.out->residual = sweep_state[1];
@@ -818,6 +831,22 @@ __global__ void __launch_bounds__(SOLVER_TPB, 1)
         a.out->inner_iters = inner_total;
         a.out->sweeps = sweep;
     }
+    __syncthreads();
+    return true;
+}
+
+template <int N, int OP>
+__global__ void __launch_bounds__(SOLVER_TPB, 1)
+    k_minres_mixed(DevMesh m, SolveArgs a, KrylovWork<float> w, MixedArgs mx)
+{
+    extern __shared__ __align__(16) unsigned char smraw[];
+    __shared__ double red[34];
+    __shared__ MinresScal<float> sc;
+    __shared__ double sweep_state[3];  // r0, |r|, done
+    __shared__ float fdmS[N * N], fdmL[N];  // element preconditioner basis
+    int eb, ee;
+    block_range(m.E, eb, ee);
+    mixed_solve<N, OP>(m, a, w, mx, eb, ee, blockIdx.x == 0, smraw, red, sc, sweep_state, fdmS, fdmL);
 }
 
 // --------------------------------------------------------- persistent PCG
