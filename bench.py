@@ -250,10 +250,16 @@ FORMS = {
                                            "guess (test relative to |b|)"),
     "mixed_fdm_learned": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
                                             "preconditioner in FP64 iterative refinement, stage guess = "
-                                            "extrapolation corrected by the BF16 network (trained on the GPU on "
-                                            "stage solves of other initial packets), residual-minimising step"),
+                                            "quadratic extrapolation corrected by the BF16 network (trained on the "
+                                            "GPU on stage solves of other initial packets), residual-minimising "
+                                            "step"),
 }
-GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1, "mixed_fdm_learned": 2}
+FORMS["mixed_fdm_extrap2"] = ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+                                                "preconditioner in FP64 iterative refinement, stage guess "
+                                                "extrapolated quadratically from the last three steps")
+GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1, "mixed_fdm_extrap2": 1,
+         "mixed_fdm_learned": 2}
+EXTRAP_ORDER = {"mixed_fdm_extrap2": 2, "mixed_fdm_learned": 2}
 # training trajectories of the learned form: packets (centre, sigma, momentum)
 # other than the workload's, on the same mesh and potential
 TRAIN_PACKETS = [((-3.0, 1.0), 1.2, (2.0, 1.0)), ((1.0, -2.0), 0.8, (-2.5, 2.0)), ((0.5, 2.5), 1.0, (1.0, -3.0))]
@@ -265,6 +271,7 @@ def set_form_options(ctx, form):
     prec, itol, pc, _ = FORMS[form]
     ctx.set_option(capi.OPT_PRECOND, pc)
     ctx.set_option(capi.OPT_STAGE_GUESS, GUESS.get(form, 0))
+    ctx.set_option(capi.OPT_EXTRAP_ORDER, EXTRAP_ORDER.get(form, 1))
     # the fast forms stop on the true FP64 residual below the reference's
     # threshold (half of it; a tenth with the element preconditioner, whose
     # extra digits cost few iterations), which keeps their states within 1e-8
@@ -519,7 +526,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--forms", default="fp64,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_learned",
+    ap.add_argument("--forms", default="fp64,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_extrap2,mixed_fdm_learned",
                     help="solver forms to time (comma list)")
     args = ap.parse_args()
     if args.impl == "reference":

@@ -74,6 +74,9 @@ enum sem_option {
                                     recurrence), 0 the two-barrier form of the FP64 solver */
     SEM_OPT_REFINE_TOL_SCALE = 9, /* mixed mode stops at |r| < s (tol |r0| + tol), s in (0,1],
                                     default 1 (the reference's test on the true residual) */
+    SEM_OPT_ADAPTIVE_INNER = 12, /* mixed mode: 1 (default) a sweep's inner tolerance is relaxed
+                                    to what the outer test still needs (x 0.3), 0 always
+                                    SEM_OPT_INNER_TOL */
     SEM_OPT_EXTRAP_ORDER = 11,   /* stage guess of SEM_GUESS_EXTRAPOLATE / _LEARNED: 1 (default)
                                     linear 2 z1 - z2, 2 quadratic 3 z1 - 3 z2 + z3 once three
                                     previous steps exist */
@@ -131,6 +134,7 @@ typedef struct {
     long long learned_accepted;     /* ... and that lowered the extrapolation's residual */
     double last_guess_residual_ratio; /* |r(guess used)| / |r(extrapolated)| of the last such stage */
     double last_guess_theta;        /* step taken along the predicted correction (1: as predicted) */
+    double learned_ratio_sum;       /* sum of |r(guess used)| / |r(extrapolated)| over learned guesses */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop
@@ -262,6 +266,20 @@ int sem_schrodinger_dirk4s5(sem_ctx* ctx, double* psi_re, double* psi_im, const 
 int sem_schrodinger_dirk4s3(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
                             double T, const sem_solver_opts* opts,
                             sem_step_callback cb, void* user, int* success);
+
+/* No counterpart in the reference (its 5-stage driver, schrodinger.hpp:138-285,
+ * only prints the embedded error estimate of :262-263).  Adaptive SDIRK4
+ * 5-stage: a step is accepted when |sum_l e_l z_l| / |psi_0| <= err_tol, the
+ * next dt is dt * clamp(0.9 (err_tol/err)^(1/4), 0.2, 2) (at most 0.9 after
+ * a rejection), the last step lands on T.  opts->dt is the first trial step.
+ * dts (host, may be NULL) receives the accepted steps' dt, up to
+ * dts_capacity of them (the sequence replays the fixed-step reference).  In
+ * mixed precision with a stage guess other than SEM_GUESS_ZERO a stage starts
+ * from the last accepted step's stage scaled by the dt ratio. */
+int sem_schrodinger_dirk4s5_adaptive(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
+                                     double T, const sem_solver_opts* opts, double err_tol,
+                                     double* dts, int dts_capacity, int* n_accepted, int* n_rejected,
+                                     sem_step_callback cb, void* user, int* success);
 
 /* ------------------------------------------- learned stage guess (device)
  * No counterpart in the reference (its stage solves start from zero,

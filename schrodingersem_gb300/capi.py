@@ -39,7 +39,7 @@ class SemStats(C.Structure):
                 ("solver_kernel_ms", C.c_double), ("solver_iterations_fp64", C.c_longlong),
                 ("solver_iterations_fp32", C.c_longlong), ("learned_guesses", C.c_longlong),
                 ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double),
-                ("last_guess_theta", C.c_double)]
+                ("last_guess_theta", C.c_double), ("learned_ratio_sum", C.c_double)]
 
 
 class SemBatchStats(C.Structure):
@@ -90,6 +90,9 @@ SIGNATURES = {
                                           STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
     "sem_schrodinger_dirk4s3": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(SemSolverOpts),
                                           STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
+    "sem_schrodinger_dirk4s5_adaptive": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(SemSolverOpts),
+                                                   C.c_double, _vp, C.c_int, C.POINTER(C.c_int),
+                                                   C.POINTER(C.c_int), STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
     "sem_learner_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.c_int, C.c_int, C.c_ulonglong]),
     "sem_learner_destroy": (C.c_int, [_vp]),
     "sem_learner_shape": (C.c_int, [_vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
@@ -121,6 +124,7 @@ SIGNATURES = {
 SEM_FLAG_METRIC_CORRECTED = 0x1
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
 OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_EXTRAP_ORDER = 7, 8, 9, 10, 11
+OPT_ADAPTIVE_INNER = 12
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

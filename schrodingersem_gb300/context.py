@@ -245,6 +245,17 @@ class Context:
               "sem_helmholtz")
         return bool(r.success), int(r.n_iter), float(r.residual)
 
+    def schrodinger_adaptive(self, psi_re, psi_im, V, T, dt0, max_iter, tol, err_tol, capacity=100000):
+        """adaptive SDIRK4 5-stage in place; returns (success, accepted dts, rejected count)"""
+        opts = SemSolverOpts(int(max_iter), float(tol), float(dt0), 0)
+        dts = np.zeros(int(capacity))
+        na, nr, ok = C.c_int(0), C.c_int(0), C.c_int(0)
+        check(self._L.sem_schrodinger_dirk4s5_adaptive(self._h, _ptr(psi_re), _ptr(psi_im), _ptr(V), float(T),
+                                                       C.byref(opts), float(err_tol), _hptr(dts), int(capacity),
+                                                       C.byref(na), C.byref(nr), capi.STEP_CALLBACK(), None,
+                                                       C.byref(ok)), "sem_schrodinger_dirk4s5_adaptive")
+        return bool(ok.value), dts[:min(na.value, capacity)].copy(), int(nr.value)
+
     def schrodinger(self, method: str, psi_re, psi_im, V, T, dt, max_iter, tol, n_steps=None, record=None):
         """Run a driver in place on psi_re/psi_im (host numpy or device
         torch).  Stops after n_steps through the callback when given;

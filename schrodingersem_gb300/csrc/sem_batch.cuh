@@ -147,6 +147,7 @@ __device__ void bdf2_instance(const BatchInst& I, const BatchArgs& ba, unsigned 
     mx.fdm = ba.fdm;
     mx.fused = 0;
     mx.outer_scale = ba.outer_scale;
+    mx.adaptive = 1;
     mixed_solve<N, OP_RES, true>(m, a, I.w, mx, 0, m.E, true, smraw, red, sc, sweep_state, fdmS, fdmL);
     // unmask(p) (schrodinger.hpp:105-106): owner copies are never written here
     for (long long idx = threadIdx.x; idx < n; idx += blockDim.x) {

@@ -221,6 +221,7 @@ struct sem_ctx {
     double outer_scale = 1.0;
     int apply_pipeline = 1;
     int extrap_order = 1;
+    int adaptive_inner = 1;
     // stage-guess history of the SDIRK drivers (persists across calls)
     long long hist_steps = 0;
     int hist_stages = 0;
@@ -801,6 +802,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
             if (!(v > 0 && v <= 1)) return fail(SEM_ERR_ARG, "refinement tolerance scale must be in (0,1]");
             c->outer_scale = v;
             return SEM_OK;
+        case SEM_OPT_ADAPTIVE_INNER:
+            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "adaptive inner tolerance must be 0 or 1");
+            c->adaptive_inner = (int)v;
+            return SEM_OK;
         case SEM_OPT_EXTRAP_ORDER:
             if (v != 1 && v != 2) return fail(SEM_ERR_ARG, "extrapolation order must be 1 or 2");
             c->extrap_order = (int)v;
@@ -1191,6 +1196,7 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     mx.pinv32 = nullptr;
     mx.fused = c->inner_fused;
     mx.outer_scale = c->outer_scale;
+    mx.adaptive = c->adaptive_inner;
     if (c->inner_fused) {
         if ((s = wsget(c, "k32_AZ", v, &w.AZ)) || (s = wsget(c, "k32_Y3", v, &w.Y3))) return s;
     }
@@ -1571,6 +1577,7 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     }
     c->stats.last_guess_residual_ratio = ratio;
     c->stats.last_guess_theta = theta;
+    c->stats.learned_ratio_sum += ratio;
     return SEM_OK;
 }
 
@@ -1828,6 +1835,128 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             return s;
     }
     if ((s = schro_publish(&r))) return s;
+    *success = ok ? 1 : 0;
+    return SEM_OK;
+}
+
+// Adaptive SDIRK4 5-stage (no counterpart in the reference, whose 5-stage
+// driver computes the embedded estimate, schrodinger.hpp:262-263, but keeps
+// dt fixed): a step is accepted when the estimate |sum_l e_l z_l| / |psi_0|
+// is at most err_tol, and the next dt is dt * clamp(0.9 (err_tol/err)^(1/4),
+// 0.2, 2) (0.2 .. 0.9 after a rejection); the last step lands on T.
+extern "C" int sem_schrodinger_dirk4s5_adaptive(sem_ctx* c, double* psi_re, double* psi_im, const double* V,
+                                                double T, const sem_solver_opts* o, double err_tol, double* dts,
+                                                int dts_capacity, int* n_accepted, int* n_rejected,
+                                                sem_step_callback cb, void* user, int* success)
+{
+    SEM_CHECK_CTX(c);
+    if (!psi_re || !psi_im || !V || !o || !success) return fail(SEM_ERR_ARG, "null argument");
+    if (!(o->dt > 0) || !(err_tol > 0) || dts_capacity < 0 || (dts_capacity > 0 && !dts))
+        return fail(SEM_ERR_ARG, "bad adaptive step arguments");
+    SchroRun r{};
+    int s = schro_begin(c, psi_re, psi_im, V, &r);
+    if (s) return s;
+    // schrodinger.hpp:228-262 (Hairer-Wanner SDIRK4, 5 stages, embedded estimate)
+    const std::vector<std::vector<double>> arow = {{},
+                                                   {0.5},
+                                                   {17.0 / 50.0, -1.0 / 25.0},
+                                                   {371.0 / 1360.0, -137.0 / 2720.0, 15.0 / 544.0},
+                                                   {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0}};
+    const double bw[5] = {25.0 / 24.0, -49.0 / 48.0, 125.0 / 16.0, -85.0 / 12.0, 0.25};
+    const double ew[5] = {-3.0 / 16.0, -27.0 / 32.0, 25.0 / 32.0, 0.0, 0.25};
+    const size_t zset = (size_t)5 * 2 * c->n;
+    double *Zs = nullptr, *b = nullptr, *err = nullptr;
+    if ((s = wsget(c, "ad_Z", 2 * zset, &Zs)) || (s = wsget(c, "drv_b2", 2 * c->n, &b)) ||
+        (s = wsget(c, "drv_err", 2 * c->n, &err)))
+        return s;
+    double* Z = Zs;
+    double* Zp = Zs + zset;  // stage solutions of the last accepted step
+    double a1 = 0, a2 = 0;
+    if ((s = dot_dev(c, r.P[0], r.P[0], &a1)) || (s = dot_dev(c, r.P[0] + c->n, r.P[0] + c->n, &a2))) return s;
+    const double pnorm = std::sqrt(a1 + a2);  // schrodinger.hpp:214
+    const bool guess = c->guess != SEM_GUESS_ZERO && c->prec == SEM_PREC_MIXED;
+    double t = 0.0, dt = o->dt, dt_prev = 0.0;
+    int acc = 0, rej = 0;
+    bool ok = true, have_prev = false;
+    while (t < T) {
+        if (T - t < dt) dt = T - t;
+        if (!(dt > 1e-14 * std::max(1.0, T))) {
+            ok = false;
+            break;
+        }
+        const double alpha = 0.25 * dt;
+        c->stats.last_step_stages = 5;
+        for (int st = 0; st < 5 && ok; ++st) {
+            ZList zl{};
+            zl.nz = st;
+            for (int l = 0; l < st; ++l) {
+                zl.z[l] = Z + (size_t)l * 2 * c->n;
+                zl.c[l] = arow[st][l];
+            }
+            if ((s = schro_rhs(&r, dt, zl, b))) return s;
+            double* z = Z + (size_t)st * 2 * c->n;
+            int x_zero = 1;
+            if (guess && have_prev) {  // the last step's stage, scaled to this dt
+                k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, dt / dt_prev,
+                                                                   Zp + (size_t)st * 2 * c->n, 0.0, nullptr, z);
+                c->stats.kernel_launches++;
+                SEM_CUDA(cudaGetLastError());
+                x_zero = 0;
+            } else {
+                SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
+            }
+            sem_solver_results res{};
+            int sw = 1;
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw))) return s;
+            c->stats.last_stage_iters[st] = res.n_iter;
+            c->stats.last_stage_sweeps[st] = sw;
+            if (!res.success) ok = false;
+        }
+        if (!ok) break;
+        ZList ze{};
+        for (int l = 0; l < 5; ++l)
+            if (ew[l] != 0.0) {
+                ze.z[ze.nz] = Z + (size_t)l * 2 * c->n;
+                ze.c[ze.nz++] = ew[l];
+            }
+        k_lincomb<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, ze, err);
+        c->stats.kernel_launches++;
+        SEM_CUDA(cudaGetLastError());
+        if ((s = dot_dev(c, err, err, &a1)) || (s = dot_dev(c, err + c->n, err + c->n, &a2))) return s;
+        const double est = std::sqrt(a1 + a2) / pnorm;
+        c->stats.last_error_estimate = est;
+        const double fac = est > 0 ? 0.9 * std::pow(err_tol / est, 0.25) : 2.0;
+        if (est <= err_tol) {
+            ZList zb{};
+            zb.nz = 5;
+            for (int l = 0; l < 5; ++l) {
+                zb.z[l] = Z + (size_t)l * 2 * c->n;
+                zb.c[l] = bw[l];
+            }
+            SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+                return launch_update<decltype(nv)::value>(c->dm, r.P[r.cur], zb, r.P[1 - r.cur], c->stream);
+            }));
+            r.cur = 1 - r.cur;
+            t += dt;
+            if (acc < dts_capacity) dts[acc] = dt;
+            ++acc;
+            std::swap(Z, Zp);
+            dt_prev = dt;
+            have_prev = true;
+            c->stats.steps_taken = acc;
+            dt *= std::min(2.0, std::max(0.2, fac));
+            if (cb) {
+                if ((s = schro_publish(&r))) return s;
+                if (cb(user, acc, psi_re, psi_im)) break;
+            }
+        } else {
+            ++rej;
+            dt *= std::min(0.9, std::max(0.2, fac));
+        }
+    }
+    if ((s = schro_publish(&r))) return s;
+    if (n_accepted) *n_accepted = acc;
+    if (n_rejected) *n_rejected = rej;
     *success = ok ? 1 : 0;
     return SEM_OK;
 }

@@ -138,6 +138,7 @@ struct MixedArgs {
     int fdm;             // element fast-diagonalisation preconditioner (Res only; uses KrylovWork::Z)
     int fused;           // inner solve with the single-barrier MINRES iteration (Res only)
     double outer_scale;  // refinement stops at |r| < outer_scale * (tol |r0| + tol)
+    int adaptive;        // inner tolerance of a sweep no tighter than the outer test needs
 };
 
 // ---- launchers, one explicit instantiation per N in sem_inst.cu -------------

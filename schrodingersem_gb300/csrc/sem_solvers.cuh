@@ -782,12 +782,20 @@ __device__ __forceinline__ bool mixed_solve(const DevMesh& m, const SolveArgs& a
         auto rhs = [&](const NodeInfo&, int, long long flat, int c) -> float { return (float)r64c[c][flat]; };
         MinresOut ir{};
         const int budget = min(mx.inner_maxit, a.maxit - inner_total);
+        // the inner solve reduces by inner_tol, or (last sweep) by no more
+        // than the outer test still needs, with a margin for the FP32
+        // estimate: a good initial guess then saves iterations, not sweeps
+        double itol = mx.inner_tol;
+        if (mx.adaptive) {
+            const double need = mx.outer_scale * (a.tol * sweep_state[0] + a.tol) / sweep_state[1];
+            itol = fmax(itol, fmin(0.3 * need, 0.5));
+        }
         bool okc = false;
         bool done_fdm = false;
         if constexpr (OP == OP_RES) {
             if (mx.fdm) {
                 okc = minres_core<N, float, OP, 2>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee, w,
-                                                   a.sync, a.timeout_ns, slot, rhs, mx.x32, budget, mx.inner_tol,
+                                                   a.sync, a.timeout_ns, slot, rhs, mx.x32, budget, itol,
                                                    0.0, ir, (const float*)nullptr, fdmS, fdmL);
                 done_fdm = true;
             }
@@ -795,24 +803,24 @@ __device__ __forceinline__ bool mixed_solve(const DevMesh& m, const SolveArgs& a
         if (done_fdm) {
         } else if constexpr (LEAN) {  // batched instances: no preconditioner or the element one
             okc = minres_core<N, float, OP, 0>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee, w, a.sync,
-                                               a.timeout_ns, slot, rhs, mx.x32, budget, mx.inner_tol, 0.0, ir,
+                                               a.timeout_ns, slot, rhs, mx.x32, budget, itol, 0.0, ir,
                                                (const float*)nullptr);
         } else if (OP == OP_RES && mx.fused)
             okc = mx.pinv32
                       ? minres_core_fused<N, float, OP, true>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb,
                                                               ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
-                                                              budget, mx.inner_tol, 0.0, ir, mx.pinv32)
+                                                              budget, itol, 0.0, ir, mx.pinv32)
                       : minres_core_fused<N, float, OP, false>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha,
                                                                eb, ee, w, a.sync, a.timeout_ns, slot, rhs, mx.x32,
-                                                               budget, mx.inner_tol, 0.0, ir, (const float*)nullptr);
+                                                               budget, itol, 0.0, ir, (const float*)nullptr);
         else
             okc = mx.pinv32
                       ? minres_core<N, float, OP, 1>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
                                                         w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
-                                                        mx.inner_tol, 0.0, ir, mx.pinv32)
+                                                        itol, 0.0, ir, mx.pinv32)
                       : minres_core<N, float, OP, 0>(sm32, kmax, red, sc, m, mx.pot32, (float)a.alpha, eb, ee,
                                                          w, a.sync, a.timeout_ns, slot, rhs, mx.x32, budget,
-                                                         mx.inner_tol, 0.0, ir, (const float*)nullptr);
+                                                         itol, 0.0, ir, (const float*)nullptr);
         if (!okc) return false;
         inner_total += ir.it;
         ++sweep;

@@ -17,7 +17,8 @@ import numpy as np
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--case", default="minres", choices=["minres", "apply"])
+    ap.add_argument("--case", default="minres", choices=["minres", "apply", "batch"])
+    ap.add_argument("--instances", type=int, default=64, help="batch: ensemble size")
     ap.add_argument("--n", type=int, default=192)
     ap.add_argument("--p", type=int, default=8)
     ap.add_argument("--maxit", type=int, default=30)
@@ -34,6 +35,29 @@ def main():
     from schrodingersem_gb300 import capi
     from schrodingersem_gb300.meshgen import gaussian_packet, structured_quads
     S.build()
+    if a.case == "batch":  # a few BDF2 steps of the seeded ensemble workload
+        from schrodingersem_gb300.batch import Batch
+        from schrodingersem_gb300.batch_bench import instance_fields, make_instances
+        from schrodingersem_gb300.meshgen import element_node_coords
+        insts = make_instances(a.instances)
+        B = Batch([(i["p"], i["coords"], i["elements"]) for i in insts])
+        z = {}
+        for pp in sorted({i["p"] for i in insts}):
+            c = S.Context(pp, coords=insts[0]["coords"], elements=insts[0]["elements"])
+            z[pp] = c.quadrature()[0]
+            c.close()
+        re, im, V = [], [], []
+        for inst in insts:
+            X, Y = element_node_coords(inst["coords"], inst["elements"], z[inst["p"]])
+            v, r, i = instance_fields(inst, X, Y)
+            re.append(torch.as_tensor(r, device="cuda"))
+            im.append(torch.as_tensor(i, device="cuda"))
+            V.append(torch.as_tensor(v, device="cuda"))
+        ok = B.bdf2(re, im, V, (a.reps - 0.5) * 2.5e-3, 2.5e-3, 200000, 1e-10)
+        st = B.stats()
+        print(f"batch: instances={a.instances} steps={a.reps} converged={sum(ok)} ms_per_step={st.kernel_ms / a.reps:.3f}"
+              f" inner_iterations={st.krylov_iterations}")
+        return
     co, el = structured_quads(a.n, box=(-8.0, 8.0, -8.0, 8.0), jitter=0.1, seed=1)
     ctx = S.Context(a.p, coords=co, elements=el)
     X, Y = ctx.node_coords()

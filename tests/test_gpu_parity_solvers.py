@@ -128,3 +128,38 @@ def test_callback_stops_and_state_visible(semlib, oracle, known):
     assert ok and [s for s, _ in rec] == [1, 2, 3]
     pr, pi, _ = om.schrodinger("dirk4s3", re, im, V, 1.0, 0.001, 20 * om.dof(), 1e-8, n_steps=3)
     assert rel_err(gr, pr) <= 1e-6
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_adaptive_dirk4s5_replays_fixed_step_reference(semlib, oracle, prec):
+    """adaptive SDIRK4-5: every accepted step's embedded estimate is within
+    the tolerance, the steps land on T, and replaying the accepted dt
+    sequence through the oracle's fixed-step 5-stage driver reproduces the
+    state"""
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.meshgen import gaussian_packet
+    co, el = structured(4, box=(-3, 3, -3, 3), jitter=0.1, seed=5)
+    p = 5
+    ctx = semlib.Context(p, coords=co, elements=el)
+    om = oracle.Mesh(p, coords=co, elements=el)
+    X, Y = om.node_coords()
+    re, im = gaussian_packet(X, Y, (-0.5, 0.2), 0.7, (2.0, 1.0))
+    V = X * X + Y * Y
+    if prec == "mixed":
+        ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+        ctx.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
+        ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_EXTRAPOLATE)
+        ctx.set_option(capi.OPT_REFINE_TOL_SCALE, 0.1)
+    T, tol, err_tol = 0.06, 1e-12, 1e-6
+    a, b = re.copy(), im.copy()
+    ok, dts, nrej = ctx.schrodinger_adaptive(a, b, V, T, 0.02, 100000, tol, err_tol)
+    assert ok and len(dts) >= 2
+    assert abs(dts.sum() - T) < 1e-12
+    assert ctx.stats().last_error_estimate <= err_tol
+    # the controller moved away from the 0.02 trial step
+    assert nrej > 0 or abs(dts[-2] - 0.02) > 1e-12
+    r, i = re.copy(), im.copy()
+    for d in dts:
+        r, i, okk = om.schrodinger("dirk4s5", r, i, V, 0.5 * d, d, 100000, 1e-13)
+        assert okk
+    assert max(rel_err(a, r), rel_err(b, i)) < 1e-8
