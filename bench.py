@@ -203,6 +203,46 @@ def cpu_baseline_sample(iters_per_step, cap=60):
                       f"step's measured {iters_per_step:.0f} MINRES iterations"}
 
 
+def _batch_cpu_worker(args):
+    """one ensemble instance on the CPU oracle (one thread): seconds per BDF2 step"""
+    inst, steps, dt, tol = args
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+    from schrodingersem_gb300.batch_bench import instance_fields
+    O.build()
+    O.set_threads(1)
+    om = O.Mesh(inst["p"], coords=inst["coords"], elements=inst["elements"])
+    X, Y = om.node_coords()
+    V, re, im = instance_fields(inst, X, Y)
+    t0 = time.perf_counter()
+    _, _, ok = om.schrodinger("bdf2", re, im, V, (steps - 0.5) * dt, dt, 20 * om.dof(), tol)
+    return (time.perf_counter() - t0) / steps, bool(ok), int(inst["n"]) ** 2 * (inst["p"] + 1) ** 2
+
+
+def batch_cpu_baseline(n_instances, sample=16, steps=2):
+    """the ensemble on the host cores: a size-stratified sample of instances,
+    one process (one thread) per instance, every core busy; the machine's
+    instance-steps/s scaled to the ensemble's mean instance size"""
+    import multiprocessing as mp
+
+    from schrodingersem_gb300.batch_bench import make_instances
+    insts = make_instances(n_instances)
+    size = [i["n"] ** 2 * (i["p"] + 1) ** 2 for i in insts]
+    order = sorted(range(len(insts)), key=lambda i: size[i])
+    pick = [order[int(round(q))] for q in np.linspace(0, len(order) - 1, min(sample, len(order)))]
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(min(cores, len(pick))) as pool:
+        res = pool.map(_batch_cpu_worker, [(insts[i], steps, 2.5e-3, 1e-10) for i in pick])
+    wall = time.perf_counter() - t0
+    s_node_step = sum(r[0] for r in res) / sum(r[2] for r in res)
+    per_inst_step = s_node_step * float(np.mean(size))
+    return {"value": cores / per_inst_step, "unit": "instance-steps/s", "cores": cores, "kind": "port",
+            "sample": f"{len(pick)} instances stratified by size, {steps} BDF2 steps each on the CPU oracle (FP64 "
+                      f"MINRES, one thread per process, {wall:.1f} s wall); rate = cores / (mean instance size x "
+                      f"measured seconds per node-step)", "all_converged": all(r[1] for r in res)}
+
+
 def apply_gbs(ctx, torch, reps=20):
     """standalone Res apply (element kernel + assembly) with L2 flushed before
     each apply: algorithmic bytes n_loc * s * 9 words per apply"""
@@ -486,6 +526,12 @@ def run_ours(args):
                  for f, r in res.items()}
     cpu = cpu_baseline_sample(res["fp64"]["iters_per_step"] if "fp64" in res else H["iters_per_step"]) \
         if not args.no_cpu else None
+    # the batched-ensemble workload (1,024 seeded instances, BDF2)
+    from schrodingersem_gb300.batch_bench import run_batch
+    batch = run_batch(1024, steps=args.batch_steps, warmup=2)
+    if not args.no_cpu:
+        batch["cpu_baseline"] = batch_cpu_baseline(1024)
+        batch["speedup_vs_cpu"] = batch["value"] / batch["cpu_baseline"]["value"]
     flops64 = n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
     line = {
         "metric": METRIC, "value": ms / 1e3, "unit": "s/step", "n_gpus": world, "steps": args.steps,
@@ -509,6 +555,7 @@ def run_ours(args):
                   "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak, "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
                   "bytes_fp64": app["fp64"]["bytes"], "note": "n_loc*s*9 words, L2 flushed before each apply"},
         "cpu_baseline": cpu,
+        "batch": batch,
         "e2e": {"value": e2e_s, "unit": "s/step", "h2d_bytes_per_step": 3 * nbytes,
                 "d2h_bytes_per_step": 2 * nbytes},
         "clocks": clk.summary(),
@@ -526,6 +573,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched-ensemble workload")
     ap.add_argument("--forms", default="fp64,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_extrap2,mixed_fdm_learned",
                     help="solver forms to time (comma list)")
     args = ap.parse_args()

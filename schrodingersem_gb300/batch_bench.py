@@ -54,6 +54,59 @@ def instance_fields(inst, X, Y):
     return 2.0 * V, re, -im
 
 
+def run_batch(n_instances: int = 1024, steps: int = 100, warmup: int = 3, seed: int = 2026):
+    """build the seeded ensemble, warm up (graph capture), time `steps` BDF2
+    steps of all instances; returns the measurement as a dict"""
+    import torch
+
+    import schrodingersem_gb300 as S
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.batch import Batch
+    from schrodingersem_gb300.meshgen import element_node_coords
+    S.build()
+    insts = make_instances(n_instances, seed)
+    t0 = time.time()
+    B = Batch([(i["p"], i["coords"], i["elements"]) for i in insts])
+    setup_s = time.time() - t0
+    B.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
+    z = {}
+    for pp in sorted({i["p"] for i in insts}):  # GLL nodes of each degree
+        c = S.Context(pp, coords=insts[0]["coords"], elements=insts[0]["elements"])
+        z[pp] = c.quadrature()[0]
+        c.close()
+    re, im, V = [], [], []
+    for inst in insts:
+        X, Y = element_node_coords(inst["coords"], inst["elements"], z[inst["p"]])
+        v, r, i = instance_fields(inst, X, Y)
+        re.append(torch.as_tensor(r, device="cuda"))
+        im.append(torch.as_tensor(i, device="cuda"))
+        V.append(torch.as_tensor(v, device="cuda"))
+    dt = 2.5e-3  # dt' = dt/2 of the workload's 5e-3
+    maxit = 200000
+    B.bdf2(re, im, V, (warmup - 0.5) * dt, dt, maxit, 1e-10)  # warm-up (graph capture)
+    s0 = B.stats()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    ok = B.bdf2(re, im, V, (steps - 0.5) * dt, dt, maxit, 1e-10)
+    torch.cuda.synchronize()
+    wall = time.time() - t0
+    s1 = B.stats()
+    ms = s1.kernel_ms - s0.kernel_ms
+    nodes = sum(i["n"] ** 2 * (i["p"] + 1) ** 2 for i in insts)
+    return {
+        "metric": "batched BDF2 instance-steps per second", "value": n_instances * steps / (ms / 1e3),
+        "unit": "instance-steps/s", "instances": n_instances, "steps": steps, "warmup": warmup,
+        "ms_per_step": ms / steps, "wall_s": wall, "setup_s": setup_s,
+        "local_nodes_per_component": nodes, "converged": int(sum(ok)),
+        "inner_iterations_per_instance_step": (s1.krylov_iterations - s0.krylov_iterations) / (n_instances * steps),
+        "graph_launches": s1.graph_launches - s0.graph_launches, "graphs_built": s1.graphs_built,
+        "kmax_of_p": {p: s1.kmax_of_p[p] for p in (4, 6, 8)},
+        "config": {"workload": f"{n_instances:,} seeded instances: n~U{{4..32}} quads on [-6,6]^2, p in {{4,6,8}}, "
+                               "6-Gaussian potentials, Gaussian packets; BDF2 dt=5e-3, MINRES 1e-10, FP32 inner + "
+                               "FP64 refinement, element preconditioner", "dtype": "f64+f32"},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--instances", type=int, default=1024)
@@ -61,58 +114,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     a = ap.parse_args()
     sys.path.insert(0, ROOT)
-    insts = make_instances(a.instances)
-    import torch
-
-    import schrodingersem_gb300 as S
-    from schrodingersem_gb300 import capi
-    from schrodingersem_gb300.batch import Batch
-    S.build()
-    t0 = time.time()
-    B = Batch([(i["p"], i["coords"], i["elements"]) for i in insts])
-    setup_s = time.time() - t0
-    B.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
-    from schrodingersem_gb300.meshgen import element_node_coords
-    z = {}
-    for pp in sorted({i["p"] for i in insts}):  # GLL nodes of each degree
-        c = S.Context(pp, coords=insts[0]["coords"], elements=insts[0]["elements"])
-        z[pp] = c.quadrature()[0]
-        c.close()
-    fields = []
-    for k, inst in enumerate(insts):
-        X, Y = element_node_coords(inst["coords"], inst["elements"], z[inst["p"]])
-        V, re, im = instance_fields(inst, X, Y)
-        fields.append((torch.as_tensor(re, device="cuda"), torch.as_tensor(im, device="cuda"),
-                       torch.as_tensor(V, device="cuda")))
-    dt = 2.5e-3  # dt' = dt/2 of the workload's 5e-3
-    maxit = 200000
-    re = [f[0] for f in fields]
-    im = [f[1] for f in fields]
-    V = [f[2] for f in fields]
-    ok = B.bdf2(re, im, V, (a.warmup - 0.5) * dt, dt, maxit, 1e-10)  # warm-up (graph capture)
-    s0 = B.stats()
-    torch.cuda.synchronize()
-    t0 = time.time()
-    ok = B.bdf2(re, im, V, (a.steps - 0.5) * dt, dt, maxit, 1e-10)
-    torch.cuda.synchronize()
-    wall = time.time() - t0
-    s1 = B.stats()
-    ms = s1.kernel_ms - s0.kernel_ms
-    nodes = sum(i["n"] ** 2 * (i["p"] + 1) ** 2 for i in insts)
-    line = {
-        "metric": "batched BDF2 instance-steps per second", "value": a.instances * a.steps / (ms / 1e3),
-        "unit": "instance-steps/s", "instances": a.instances, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": ms / a.steps, "wall_s": wall, "setup_s": setup_s,
-        "local_nodes_per_component": nodes, "converged": int(sum(ok)),
-        "inner_iterations_per_instance_step": (s1.krylov_iterations - s0.krylov_iterations) /
-                                              (a.instances * a.steps),
-        "graph_launches": s1.graph_launches - s0.graph_launches, "graphs_built": s1.graphs_built,
-        "kmax_of_p": {p: s1.kmax_of_p[p] for p in (4, 6, 8)},
-        "config": {"workload": "1,024 seeded instances: n~U{4..32} quads on [-6,6]^2, p in {4,6,8}, 6-Gaussian "
-                               "potentials, Gaussian packets; BDF2 dt=5e-3, MINRES 1e-10, FP32 inner + FP64 "
-                               "refinement, element preconditioner", "dtype": "f64+f32"},
-    }
-    print(json.dumps(line))
+    print(json.dumps(run_batch(a.instances, a.steps, a.warmup)))
 
 
 if __name__ == "__main__":

@@ -245,15 +245,19 @@ class Context:
               "sem_helmholtz")
         return bool(r.success), int(r.n_iter), float(r.residual)
 
-    def schrodinger_adaptive(self, psi_re, psi_im, V, T, dt0, max_iter, tol, err_tol, capacity=100000):
-        """adaptive SDIRK4 5-stage in place; returns (success, accepted dts, rejected count)"""
+    def schrodinger_adaptive(self, psi_re, psi_im, V, T, dt0, max_iter, tol, err_tol, capacity=100000,
+                             n_steps=None):
+        """adaptive SDIRK4 5-stage in place (stops after n_steps accepted steps
+        when given); returns (success, accepted dts, rejected count)"""
         opts = SemSolverOpts(int(max_iter), float(tol), float(dt0), 0)
         dts = np.zeros(int(capacity))
         na, nr, ok = C.c_int(0), C.c_int(0), C.c_int(0)
+        cb = (capi.STEP_CALLBACK(lambda user, step, a, b: 1 if step >= n_steps else 0) if n_steps
+              else capi.STEP_CALLBACK())
         check(self._L.sem_schrodinger_dirk4s5_adaptive(self._h, _ptr(psi_re), _ptr(psi_im), _ptr(V), float(T),
                                                        C.byref(opts), float(err_tol), _hptr(dts), int(capacity),
-                                                       C.byref(na), C.byref(nr), capi.STEP_CALLBACK(), None,
-                                                       C.byref(ok)), "sem_schrodinger_dirk4s5_adaptive")
+                                                       C.byref(na), C.byref(nr), cb, None, C.byref(ok)),
+              "sem_schrodinger_dirk4s5_adaptive")
         return bool(ok.value), dts[:min(na.value, capacity)].copy(), int(nr.value)
 
     def schrodinger(self, method: str, psi_re, psi_im, V, T, dt, max_iter, tol, n_steps=None, record=None):

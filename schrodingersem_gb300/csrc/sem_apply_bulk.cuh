@@ -108,10 +108,11 @@ __host__ __device__ constexpr int bulk_arrays()
            ((OP == OP_HELM || OP == OP_RES || OP == OP_F) ? 1 : 0);
 }
 
-template <typename T>
+// threads per block: one per element line and component
+template <typename T, int OP>
 __host__ __device__ constexpr int bulk_tpb()
 {
-    return sizeof(T) == 4 ? 256 : 128;
+    return (sizeof(T) == 4 ? 256 : 128) * op_nc<OP>();
 }
 
 constexpr int BULK_STAGES = 2;  // one batch in flight while one computes (3 measured slower)
@@ -125,7 +126,7 @@ template <typename T, int OP>
 __host__ __device__ constexpr int bulk_k(int N)
 {
     const int q = sizeof(T) == 4 ? 4 : 2;
-    const int by_lines = bulk_tpb<T>() / N;
+    const int by_lines = bulk_tpb<T, OP>() / op_nc<OP>() / N;
     const int per_node = (BULK_STAGES * bulk_arrays<OP>() + 2 * op_nc<OP>()) * (int)sizeof(T);
     const int by_smem = (int)(BULK_SMEM_TARGET / (size_t)(per_node * N * N));
     const int k = (by_lines < by_smem ? by_lines : by_smem) / q * q;
@@ -158,7 +159,7 @@ struct DMat {
 // accumulation runs over k in ascending order as in apply_range, so both
 // kernels give the same bits.
 template <int N, typename T, int OP, bool GATHER>
-__global__ void __launch_bounds__(bulk_tpb<T>())
+__global__ void __launch_bounds__(bulk_tpb<T, OP>())
     k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
                  const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk,
                  long long timeout_ns)
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(bulk_tpb<T>())
     // (ring_src).  The table entries and values of a block's next batch are
     // loaded into registers while the current batch computes.
     constexpr int R = 4 * (N - 1);
-    constexpr int TPB = bulk_tpb<T>();
+    constexpr int TPB = bulk_tpb<T, OP>();
     constexpr int GQ = (K * R + TPB - 1) / TPB;
     int gsrc[GQ];
     T gval[GQ][NC];
@@ -297,134 +298,113 @@ __global__ void __launch_bounds__(bulk_tpb<T>())
         if (OP == OP_MASS) {
             for (int t = threadIdx.x; t < total; t += blockDim.x) y0[(long long)e0 * NN + t] = st[A_MASS * BN + t] * st[t];
         } else {
-            // large elements keep ur in W2 and the components' laplacians in
-            // W2 between uses instead of in registers
-            constexpr bool LOWREG = N * NC * sizeof(T) > 128;
-            const int line = threadIdx.x;
+            // thread t works on component c = t / LP, line t % LP
+            constexpr int LP = TPB / NC;
+            const int c = threadIdx.x / LP;
+            const int line = threadIdx.x - c * LP;
             const bool act = line < ne * N;
             const int le = line / N, l = line - (line / N) * N;
             const int base = le * NN;
-            T ur[LOWREG ? 1 : NC][N];
-            if (LOWREG) {  // W2 is written in P1
-                if (threadIdx.x == 0 && store_bulk) bulk_wait_read();
-                __syncthreads();
-            }
-            // ---- P1
-            if (act) {
-#pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    const T* uc = st + c * BN + base;
-                    T* urc = ur[LOWREG ? 0 : c];
-                    T v[N], acc[N];
-#pragma unroll
-                    for (int i = 0; i < N; ++i) {
-                        v[i] = uc[l * N + i];
-                        urc[i] = T(0);
-                    }
-#pragma unroll
-                    for (int k = 0; k < N; ++k)
-#pragma unroll
-                        for (int i = 0; i < N; ++i) urc[i] = fma(D.d[i * N + k], v[k], urc[i]);
-                    if (LOWREG) {
-#pragma unroll
-                        for (int i = 0; i < N; ++i) W2[c * BN + base + l * N + i] = urc[i];
-                    }
-#pragma unroll
-                    for (int j = 0; j < N; ++j) {
-                        v[j] = uc[j * N + l];
-                        acc[j] = T(0);
-                    }
-#pragma unroll
-                    for (int k = 0; k < N; ++k)
-#pragma unroll
-                        for (int j = 0; j < N; ++j) acc[j] = fma(D.d[j * N + k], v[k], acc[j]);
-#pragma unroll
-                    for (int j = 0; j < N; ++j) W1[c * BN + base + j * N + l] = acc[j];
-                }
-            }
-            if (!LOWREG && threadIdx.x == 0 && store_bulk) bulk_wait_read();  // W2 of the previous batch read out
+            T* w1 = W1 + c * BN + base;
+            T* w2 = W2 + c * BN + base;
+            // W1 is written below and was the previous batch's bulk-store source
+            if (threadIdx.x == 0 && store_bulk) bulk_wait_read();
             __syncthreads();
-            // ---- P2
+            T ur[N];
+            // ---- P1: column l -> ur (registers); row l -> us (W1)
             if (act) {
-                T g11[N], g12[N], g22[N];
+                const T* uc = st + c * BN + base;
+                T v[N], acc[N];
 #pragma unroll
                 for (int i = 0; i < N; ++i) {
-                    g11[i] = st[A_G11 * BN + base + l * N + i];
-                    g12[i] = st[(A_G11 + 1) * BN + base + l * N + i];
-                    g22[i] = st[(A_G11 + 2) * BN + base + l * N + i];
+                    v[i] = uc[l * N + i];
+                    ur[i] = T(0);
                 }
 #pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    T f1[N], acc[N];
+                for (int k = 0; k < N; ++k)
 #pragma unroll
-                    for (int i = 0; i < N; ++i) {
-                        const T us = W1[c * BN + base + l * N + i];
-                        const T urv = LOWREG ? W2[c * BN + base + l * N + i] : ur[LOWREG ? 0 : c][i];
-                        f1[i] = g11[i] * urv - g12[i] * us;
-                        W1[c * BN + base + l * N + i] = g22[i] * us - g12[i] * urv;
-                        acc[i] = T(0);
-                    }
+                    for (int i = 0; i < N; ++i) ur[i] = fma(D.d[i * N + k], v[k], ur[i]);
 #pragma unroll
-                    for (int k = 0; k < N; ++k)
-#pragma unroll
-                        for (int i = 0; i < N; ++i) acc[i] = fma(D.d[k * N + i], f1[k], acc[i]);
-#pragma unroll
-                    for (int i = 0; i < N; ++i) W2[c * BN + base + l * N + i] = acc[i];
+                for (int j = 0; j < N; ++j) {
+                    v[j] = uc[j * N + l];
+                    acc[j] = T(0);
                 }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int j = 0; j < N; ++j) acc[j] = fma(D.d[j * N + k], v[k], acc[j]);
+#pragma unroll
+                for (int j = 0; j < N; ++j) w1[j * N + l] = acc[j];
             }
             __syncthreads();
-            // ---- P3: row l, all components (the Res/f epilogue mixes them)
+            // ---- P2: column l: fluxes; f2 -> W1, lap1 = D^T f1 -> W2
             if (act) {
-                T lapr[LOWREG ? 1 : NC][N];
+                T f1[N], acc[N];
 #pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    T f2[N];
-                    T* lc = lapr[LOWREG ? 0 : c];
-#pragma unroll
-                    for (int j = 0; j < N; ++j) {
-                        lc[j] = W2[c * BN + base + j * N + l];
-                        f2[j] = W1[c * BN + base + j * N + l];
-                    }
-#pragma unroll
-                    for (int k = 0; k < N; ++k)
-#pragma unroll
-                        for (int j = 0; j < N; ++j) lc[j] = fma(D.d[k * N + j], f2[k], lc[j]);
-                    if (LOWREG) {
-#pragma unroll
-                        for (int j = 0; j < N; ++j) W2[c * BN + base + j * N + l] = lc[j];
-                    }
+                for (int i = 0; i < N; ++i) {
+                    const int q = base + l * N + i;
+                    const T g11 = st[A_G11 * BN + q], g12 = st[(A_G11 + 1) * BN + q], g22 = st[(A_G11 + 2) * BN + q];
+                    const T us = w1[l * N + i];
+                    f1[i] = g11 * ur[i] - g12 * us;
+                    w1[l * N + i] = g22 * us - g12 * ur[i];
+                    acc[i] = T(0);
                 }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int i = 0; i < N; ++i) acc[i] = fma(D.d[k * N + i], f1[k], acc[i]);
+#pragma unroll
+                for (int i = 0; i < N; ++i) w2[l * N + i] = acc[i];
+            }
+            __syncthreads();
+            // ---- P3: row l: lap = lap1 + f2 D -> W2 (in place)
+            if (act) {
+                T lap[N], f2[N];
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    lap[j] = w2[j * N + l];
+                    f2[j] = w1[j * N + l];
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int j = 0; j < N; ++j) lap[j] = fma(D.d[k * N + j], f2[k], lap[j]);
+#pragma unroll
+                for (int j = 0; j < N; ++j) w2[j * N + l] = lap[j];
+            }
+            __syncthreads();
+            // ---- P4: row l, component c of the operator (the Res/f
+            // combination reads the other component's laplacian) -> W1
+            if (act) {
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     const int q = base + j * N + l;
-                    T lap[NC][1];
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) lap[c][0] = LOWREG ? W2[c * BN + q] : lapr[LOWREG ? 0 : c][j];
-                    T o[NC];
+                    T o;
                     if (OP == OP_LAPLACE) {
-                        o[0] = lap[0][0];
+                        o = W2[q];
                     } else {
                         const T ms = st[A_MASS * BN + q];
                         const T pv = (OP == OP_HELM || OP == OP_RES || OP == OP_F) ? st[A_POT * BN + q] : T(0);
-                        T u[NC];
-#pragma unroll
-                        for (int c = 0; c < NC; ++c) u[c] = st[c * BN + q];
                         if (OP == OP_HELM) {
-                            o[0] = lap[0][0] + (ms * pv) * u[0];
-                        } else if (OP == OP_RES) {
+                            o = W2[q] + (ms * pv) * st[q];
+                        } else {
                             const T mv = ms * pv;
-                            const T Lv = lap[NC - 1][0] + mv * u[NC - 1];
-                            const T Lu = lap[0][0] + mv * u[0];
-                            o[0] = ms * u[0] + alpha * Lv;
-                            o[NC - 1] = alpha * Lu - ms * u[NC - 1];
-                        } else {  // OP_F
-                            const T mv = ms * pv;
-                            o[0] = -(lap[NC - 1][0] + mv * u[NC - 1]);
-                            o[NC - 1] = -(lap[0][0] + mv * u[0]);
+                            const T u0 = st[q], u1 = st[(NC - 1) * BN + q];
+                            const T lap0 = W2[q], lap1 = W2[(NC - 1) * BN + q];
+                            if (OP == OP_RES) {
+                                if (c == 0) {
+                                    const T Lv = lap1 + mv * u1;
+                                    o = ms * u0 + alpha * Lv;
+                                } else {
+                                    const T Lu = lap0 + mv * u0;
+                                    o = alpha * Lu - ms * u1;
+                                }
+                            } else {  // OP_F
+                                o = (c == 0) ? -(lap1 + mv * u1) : -(lap0 + mv * u0);
+                            }
                         }
                     }
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) W2[c * BN + q] = o[c];
+                    W1[c * BN + q] = o;
                 }
             }
             fence_proxy_async_smem();
@@ -432,14 +412,14 @@ __global__ void __launch_bounds__(bulk_tpb<T>())
             if (store_bulk && b < nfull) {
                 if (threadIdx.x == 0) {
 #pragma unroll
-                    for (int c = 0; c < NC; ++c)
-                        bulk_store(outp[c] + (long long)e0 * NN, W2 + c * BN, (uint32_t)(BN * sizeof(T)));
+                    for (int cc = 0; cc < NC; ++cc)
+                        bulk_store(outp[cc] + (long long)e0 * NN, W1 + cc * BN, (uint32_t)(BN * sizeof(T)));
                     bulk_commit();
                 }
             } else {
                 for (int t = threadIdx.x; t < total; t += blockDim.x)
 #pragma unroll
-                    for (int c = 0; c < NC; ++c) outp[c][(long long)e0 * NN + t] = W2[c * BN + t];
+                    for (int cc = 0; cc < NC; ++cc) outp[cc][(long long)e0 * NN + t] = W1[cc * BN + t];
             }
         }
         // stage s free; this thread's shared-memory accesses ordered before
@@ -466,7 +446,7 @@ cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         int nb = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER>, bulk_tpb<T>(),
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER>, bulk_tpb<T, OP>(),
                                                                 smem)) != cudaSuccess)
             return e;
         blocks_per_sm = nb;
@@ -480,7 +460,7 @@ cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T
     const int grid = (int)std::min<long long>(nbatch, (long long)sms * blocks_per_sm);
     const int store_bulk = (((uintptr_t)y0 | (uintptr_t)(y1 ? y1 : y0)) & 15u) == 0;
     k_apply_bulk<N, T, OP, GATHER>
-        <<<grid, bulk_tpb<T>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, timeout_ns);
+        <<<grid, bulk_tpb<T, OP>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, timeout_ns);
     return cudaGetLastError();
 }
 

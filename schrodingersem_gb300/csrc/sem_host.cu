@@ -1880,7 +1880,7 @@ extern "C" int sem_schrodinger_dirk4s5_adaptive(sem_ctx* c, double* psi_re, doub
     bool ok = true, have_prev = false;
     while (t < T) {
         if (T - t < dt) dt = T - t;
-        if (!(dt > 1e-14 * std::max(1.0, T))) {
+        if (!(dt > 1e-10 * o->dt)) {  // the controller cannot reach the tolerance
             ok = false;
             break;
         }
