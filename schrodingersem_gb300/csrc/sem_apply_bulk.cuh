@@ -112,11 +112,11 @@ __host__ __device__ constexpr int bulk_arrays()
 template <typename T, int OP>
 __host__ __device__ constexpr int bulk_tpb()
 {
-    return (sizeof(T) == 4 ? 256 : 128) * op_nc<OP>();
+    return (sizeof(T) == 4 ? 128 : 64) * op_nc<OP>();
 }
 
 constexpr int BULK_STAGES = 2;  // one batch in flight while one computes (3 measured slower)
-constexpr size_t BULK_SMEM_TARGET = 200 * 1024;
+constexpr size_t BULK_SMEM_TARGET = 72 * 1024;  // three blocks per SM
 
 // elements per batch: one line thread per element column (K N <= threads),
 // BULK_STAGES stages of every staged array plus two work planes per

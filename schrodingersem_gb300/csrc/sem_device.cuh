@@ -283,12 +283,33 @@ __device__ __forceinline__ void load_dmat_raw(T* sm, const DevMesh& m)
     for (int t = threadIdx.x; t < N * N; t += blockDim.x) sm[t] = D[t];
 }
 
+template <int N, typename T, int OP, bool POST, class Load, class Post, class Store>
+__device__ __forceinline__ void apply_range_post(T* sm, int kmax, const Fac<T>& fac,
+                                                 const T* __restrict__ pot, T alpha, int e0, int ne,
+                                                 Load&& load, Post&& post, Store&& store);
+
 // One block-wide pass over elements [e0, e0+ne), ne <= kmax.  Every thread
 // of the block must call it.  Same operator and callbacks as apply_chunk.
 template <int N, typename T, int OP, class Load, class Store>
 __device__ __forceinline__ void apply_range(T* sm, int kmax, const Fac<T>& fac,
                                             const T* __restrict__ pot, T alpha, int e0, int ne,
                                             Load&& load, Store&& store)
+{
+    apply_range_post<N, T, OP, false>(
+        sm, kmax, fac, pot, alpha, e0, ne,
+        [&](int e, int i, int j, long long flat, T* u, T*) { load(e, i, j, flat, u); },
+        [&](int, int, int, long long, const T*, const T*) {}, store);
+}
+
+// apply_range with the input split in two: load(e,i,j,flat,u,aux) computes
+// the staged inputs u and per-node values aux without writing global memory,
+// so the loads of several nodes overlap; post(e,i,j,flat,u,aux) then does the
+// caller's global stores for the node (aux is parked in the flux area, free
+// until the flux phase).
+template <int N, typename T, int OP, bool POST, class Load, class Post, class Store>
+__device__ __forceinline__ void apply_range_post(T* sm, int kmax, const Fac<T>& fac,
+                                                 const T* __restrict__ pot, T alpha, int e0, int ne,
+                                                 Load&& load, Post&& post, Store&& store)
 {
     constexpr int NN = N * N;
     constexpr int NC = op_nc<OP>();
@@ -304,10 +325,27 @@ __device__ __forceinline__ void apply_range(T* sm, int kmax, const Fac<T>& fac,
         const int le = t / NN;
         const int node = t - le * NN;
         const int e = e0 + le;
-        T u[NC];
-        load(e, node % N, node / N, (long long)e * NN + node, u);
+        T u[NC], aux[NC];
+        load(e, node % N, node / N, (long long)e * NN + node, u, aux);
 #pragma unroll
-        for (int c = 0; c < NC; ++c) su[c * st + t] = u[c];
+        for (int c = 0; c < NC; ++c) {
+            su[c * st + t] = u[c];
+            if (POST) sf1[c * st + t] = aux[c];
+        }
+    }
+    if (POST) {
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int le = t / NN;
+            const int node = t - le * NN;
+            const int e = e0 + le;
+            T u[NC], aux[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                u[c] = su[c * st + t];
+                aux[c] = sf1[c * st + t];
+            }
+            post(e, node % N, node / N, (long long)e * NN + node, u, aux);
+        }
     }
     __syncthreads();
     if (OP == OP_MASS) {
@@ -438,9 +476,25 @@ __device__ __forceinline__ void load_fdm_basis(T* S, T* lam, const DevMesh& m)
 // Every thread of the block must call it.  S (S(i,k) at [i*N+k]) and lam
 // are in shared memory; the staging area sm uses the apply's u/f1 regions
 // (2 NC kmax N^2 values after the first N^2).
+template <int N, typename T, int NC, bool POST, class Load, class Post, class Store>
+__device__ __forceinline__ void fdm_range_post(T* sm, int kmax, const T* S, const T* lam, const DevMesh& m,
+                                               T alpha, int e0, int ne, Load&& load, Post&& post, Store&& store);
+
 template <int N, typename T, int NC, class Load, class Store>
 __device__ __forceinline__ void fdm_range(T* sm, int kmax, const T* S, const T* lam, const DevMesh& m, T alpha,
                                           int e0, int ne, Load&& load, Store&& store)
+{
+    fdm_range_post<N, T, NC, false>(
+        sm, kmax, S, lam, m, alpha, e0, ne,
+        [&](int e, int i, int j, long long flat, T* u, T*) { load(e, i, j, flat, u); },
+        [&](int, int, int, long long, const T*, const T*) {}, store);
+}
+
+// fdm_range with the input split as in apply_range_post (aux parked in the
+// second staging area, free until the first contraction)
+template <int N, typename T, int NC, bool POST, class Load, class Post, class Store>
+__device__ __forceinline__ void fdm_range_post(T* sm, int kmax, const T* S, const T* lam, const DevMesh& m,
+                                               T alpha, int e0, int ne, Load&& load, Post&& post, Store&& store)
 {
     constexpr int NN = N * N;
     const int total = ne * NN;
@@ -453,10 +507,27 @@ __device__ __forceinline__ void fdm_range(T* sm, int kmax, const T* S, const T* 
         const int le = t / NN;
         const int node = t - le * NN;
         const int e = e0 + le;
-        T u[NC];
-        load(e, node % N, node / N, (long long)e * NN + node, u);
+        T u[NC], aux[NC];
+        load(e, node % N, node / N, (long long)e * NN + node, u, aux);
 #pragma unroll
-        for (int c = 0; c < NC; ++c) su[c * st + t] = u[c];
+        for (int c = 0; c < NC; ++c) {
+            su[c * st + t] = u[c];
+            if (POST) stt[c * st + t] = aux[c];
+        }
+    }
+    if (POST) {
+        for (int t = threadIdx.x; t < total; t += blockDim.x) {
+            const int le = t / NN;
+            const int node = t - le * NN;
+            const int e = e0 + le;
+            T u[NC], aux[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) {
+                u[c] = su[c * st + t];
+                aux[c] = stt[c * st + t];
+            }
+            post(e, node % N, node / N, (long long)e * NN + node, u, aux);
+        }
     }
     __syncthreads();
     // 1. t(a,j) = sum_i S(i,a) u(i,j)

@@ -288,31 +288,59 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
             const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
             const T* Ycur = w.Y[(it - 1) & 1];
             T s1 = T(0);
-#pragma unroll 4
-            for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x) {
-                const int e = (int)(idx / NN);
-                const int node = (int)(idx - (long long)e * NN);
-                const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
-                const bool own = ni_owner(ni);
-                const T pv = PRE == 1 ? pinv[idx] : T(1);
+            // two nodes per thread and pass: every load of both is issued
+            // before the first store (the stores may alias the loaded
+            // vectors as far as the compiler knows)
+            constexpr int U = 1;
+            const T* Zc = PRE == 2 ? w.Z[(it - 1) & 1] : L[ir2];
+            const T* Zq = PRE == 2 ? w.Z[it & 1] : nullptr;
+            for (long long i0 = nb + threadIdx.x; i0 < ne; i0 += U * (long long)blockDim.x) {
+                long long ix[U];
+                bool val[U], own[U];
+                T av[U][NC], r1v[U][NC], zc[U][NC], zp[U][NC], w1v[U][NC], w2v[U][NC], pv[U];
 #pragma unroll
-                for (int c = 0; c < NC; ++c) {
-                    const long long q = c * n + idx;
-                    const T av = dss_value<N, T, DSS_CONT>(m, Ycur + c * n, ni, e, idx) * inv_b;
-                    T y3 = av;
-                    T r1v = T(0);
-                    if (it >= 2) {
-                        r1v = L[ir1][q];
-                        y3 = av - c1 * r1v;
+                for (int u = 0; u < U; ++u) {
+                    ix[u] = i0 + u * (long long)blockDim.x;
+                    val[u] = ix[u] < ne;
+                    own[u] = false;
+                    if (!val[u]) continue;
+                    const long long idx = ix[u];
+                    const int e = (int)(idx / NN);
+                    const int node = (int)(idx - (long long)e * NN);
+                    const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+                    own[u] = ni_owner(ni);
+                    pv[u] = PRE == 1 ? pinv[idx] : T(1);
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const long long q = c * n + idx;
+                        av[u][c] = dss_value<N, T, DSS_CONT>(m, Ycur + c * n, ni, e, idx);
+                        r1v[u][c] = it >= 2 ? L[ir1][q] : T(0);
+                        zc[u][c] = Zc[q];
+                        if (pending) {
+                            zp[u][c] = PRE == 2 ? Zq[q] : T(0);
+                            w1v[u][c] = W[iw1][q];
+                            w2v[u][c] = W[iw2][q];
+                        }
                     }
-                    const T vv = inv_b * (PRE == 2 ? w.Z[(it - 1) & 1][q] : PRE == 1 ? pv * L[ir2][q] : L[ir2][q]);
-                    if (own) s1 = fma(vv, y3, s1);
-                    L[iy][q] = y3;
-                    if (pending) {
-                        const T vprev = tpinvb * (PRE == 2 ? w.Z[it & 1][q] : PRE == 1 ? pv * r1v : r1v);
-                        const T wn = tpg * ((vprev - tpeps * W[iw1][q]) - tpdelta * W[iw2][q]);
-                        W[iw][q] = wn;
-                        if (own) xp[c][idx] += tpphi * wn;
+                }
+#pragma unroll
+                for (int u = 0; u < U; ++u) {
+                    if (!val[u]) continue;
+                    const long long idx = ix[u];
+#pragma unroll
+                    for (int c = 0; c < NC; ++c) {
+                        const long long q = c * n + idx;
+                        const T a = av[u][c] * inv_b;
+                        const T y3 = it >= 2 ? a - c1 * r1v[u][c] : a;
+                        const T vv = inv_b * (PRE == 1 ? pv[u] * zc[u][c] : zc[u][c]);
+                        if (own[u]) s1 = fma(vv, y3, s1);
+                        L[iy][q] = y3;
+                        if (pending) {
+                            const T vprev = tpinvb * (PRE == 2 ? zp[u][c] : PRE == 1 ? pv[u] * r1v[u][c] : r1v[u][c]);
+                            const T wn = tpg * ((vprev - tpeps * w1v[u][c]) - tpdelta * w2v[u][c]);
+                            W[iw][q] = wn;
+                            if (own[u]) xp[c][idx] += tpphi * wn;
+                        }
                     }
                 }
             }
@@ -341,17 +369,21 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                 // Phase B above); after the barrier z = DSS -> Z[it & 1]
                 T* Zl = w.Y[(it - 1) & 1];
                 for (int e0 = eb; e0 < ee; e0 += kmax)
-                    fdm_range<N, T, NC>(
+                    fdm_range_post<N, T, NC, true>(
                         sm, kmax, fS, fL, m, alpha, e0, min(kmax, ee - e0),
-                        [&](int e, int i, int j, long long flat, T* u) {
+                        [&](int e, int i, int j, long long flat, T* u, T* aux) {
                             const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 const long long q = c * n + flat;
                                 const T y5 = L[iy][q] - c2 * L[ir2][q];
-                                L[iy][q] = y5;
+                                aux[c] = y5;
                                 u[c] = wt * y5;
                             }
+                        },
+                        [&](int, int, int, long long flat, const T*, const T* aux) {
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) L[iy][c * n + flat] = aux[c];
                         },
                         [&](int e, int i, int j, long long flat, const T* z) {
                             const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
@@ -361,36 +393,46 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                 if (!grid_barrier(gs, tmo)) return false;
                 T* Zn = w.Z[it & 1];
                 for (int e0 = eb; e0 < ee; e0 += kmax)
-                    apply_range<N, T, OP>(
+                    apply_range_post<N, T, OP, true>(
                         sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
-                        [&](int e, int i, int j, long long flat, T* u) {
+                        [&](int e, int i, int j, long long flat, T* u, T* aux) {
                             const NodeInfo ni = node_info<N>(m, e, i, j);
-                            const bool own = ni_owner(ni);
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 const long long q = c * n + flat;
-                                const T z = dss_value<N, T, DSS_CONT>(m, Zl + c * n, ni, e, flat);
-                                Zn[q] = z;
-                                u[c] = z;
-                                if (own) ss = fma(L[iy][q], z, ss);
+                                u[c] = dss_value<N, T, DSS_CONT>(m, Zl + c * n, ni, e, flat);
+                                aux[c] = L[iy][q];
+                            }
+                        },
+                        [&](int e, int i, int j, long long flat, const T* u, const T* aux) {
+                            const bool own = ni_owner(node_info<N>(m, e, i, j));
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) {
+                                Zn[c * n + flat] = u[c];
+                                if (own) ss = fma(aux[c], u[c], ss);
                             }
                         },
                         store_y(Ynext));
             } else {
                 for (int e0 = eb; e0 < ee; e0 += kmax)
-                    apply_range<N, T, OP>(
+                    apply_range_post<N, T, OP, true>(
                         sm, kmax, fac, pot, alpha, e0, min(kmax, ee - e0),
-                        [&](int e, int i, int j, long long flat, T* u) {
-                            const bool own = ni_owner(node_info<N>(m, e, i, j));
+                        [&](int, int, int, long long flat, T* u, T* aux) {
                             const T pv = PRE == 1 ? pinv[flat] : T(1);
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 const long long q = c * n + flat;
                                 const T y5 = L[iy][q] - c2 * L[ir2][q];
-                                L[iy][q] = y5;
-                                const T z = PRE == 1 ? pv * y5 : y5;  // y = precond(r2), minres.hpp:60
-                                u[c] = z;
-                                if (own) ss = fma(y5, z, ss);
+                                aux[c] = y5;
+                                u[c] = PRE == 1 ? pv * y5 : y5;  // y = precond(r2), minres.hpp:60
+                            }
+                        },
+                        [&](int e, int i, int j, long long flat, const T* u, const T* aux) {
+                            const bool own = ni_owner(node_info<N>(m, e, i, j));
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) {
+                                L[iy][c * n + flat] = aux[c];
+                                if (own) ss = fma(aux[c], u[c], ss);
                             }
                         },
                         store_y(Ynext));
