@@ -290,7 +290,7 @@ FORMS = {
                                            "guess (test relative to |b|)"),
     "mixed_fdm_learned": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
                                             "preconditioner in FP64 iterative refinement, stage guess = "
-                                            "quadratic extrapolation corrected by the BF16 network (trained on the "
+                                            "linear extrapolation corrected by the BF16 network (trained on the "
                                             "GPU on stage solves of other initial packets), residual-minimising "
                                             "step"),
 }
@@ -299,7 +299,7 @@ FORMS["mixed_fdm_extrap2"] = ("mixed", 1e-4, 2, "FP32-inner MINRES with the elem
                                                 "extrapolated quadratically from the last three steps")
 GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1, "mixed_fdm_extrap2": 1,
          "mixed_fdm_learned": 2}
-EXTRAP_ORDER = {"mixed_fdm_extrap2": 2, "mixed_fdm_learned": 2}
+EXTRAP_ORDER = {"mixed_fdm_extrap2": 2}
 # training trajectories of the learned form: packets (centre, sigma, momentum)
 # other than the workload's, on the same mesh and potential
 TRAIN_PACKETS = [((-3.0, 1.0), 1.2, (2.0, 1.0)), ((1.0, -2.0), 0.8, (-2.5, 2.0)), ((0.5, 2.5), 1.0, (1.0, -3.0))]
@@ -473,7 +473,10 @@ def run_ours(args):
         r["rel_err_vs_plain_fp64"] = rel(r["state"], res["fp64"]["state"]) if "fp64" in res else None
         r["norm_drift"] = abs(mass_norm(J, w, *r["state"]) - 1.0)
     valid = [f for f in forms if res[f]["rel_err_vs_fp64"] <= 1e-8]
-    head = min(valid, key=lambda f: res[f]["ms"])
+    best = min(valid, key=lambda f: res[f]["ms"])
+    # the metric is the learned-warm-start + FP32-inner form's step time; the
+    # fastest form within the accuracy bar is reported beside it
+    head = "mixed_fdm_learned" if "mixed_fdm_learned" in valid else best
     H = res[head]
     ms = H["ms"]
     if dist:
@@ -537,12 +540,14 @@ def run_ours(args):
         "metric": METRIC, "value": ms / 1e3, "unit": "s/step", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if prec == "fp64" else "f64+f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "form": FORMS[head][3],
+        "config": {"workload": WORKLOAD, "form": head + ": " + FORMS[head][3],
                    "accuracy": f"M-weighted relative L2 of the state after warm-up + timed steps against the FP64 "
                                f"solver at MINRES tolerance {ORACLE_TOL:g} (headline forms must stay within 1e-8)",
                    "l2": "flushed before every step (256 MiB write)", "parallelism": "replicas only"},
         "forms": forms_out,
         "speedup_vs_plain_fp64": (res["fp64"]["ms"] / ms) if "fp64" in res else None,
+        "fastest_form": {"form": best, "s_per_step": res[best]["ms"] / 1e3,
+                         "speedup_vs_plain_fp64": (res["fp64"]["ms"] / res[best]["ms"]) if "fp64" in res else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
                      "kernel": kern + " (persistent cooperative solver)",

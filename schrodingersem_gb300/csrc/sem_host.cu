@@ -1532,11 +1532,15 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     SEM_CUDA(cudaMemcpyAsync(zx, z, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
     *zext = zx;
     if ((s = guess_residual(c, V, alpha, b, zx, r))) return s;
+    double n_ext = 0;
+    if ((s = norm2_planes(c, r, &n_ext))) return s;
     LearnArgs a{};
     a.what = LEARN_FEATURES;
     a.r = r;
     a.V = V;
     a.alpha = alpha;
+    // per-element scale floor: 1e-6 of the residual's RMS over all copies
+    a.rho_floor = std::max(1e-6 * std::sqrt(n_ext / (2.0 * (double)c->n)), 1e-300);
     a.x = x;
     a.sigma = sig;
     if ((s = launch_learn_op(c, a))) return s;
@@ -1559,8 +1563,8 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     // minimal residual along the predicted correction d = z_l - z_ext:
     // r(theta) = r_ext - theta A d with A d = r_ext - r_l, so
     // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|
-    double n_ext = 0, n_l = 0, x1 = 0, x2 = 0;
-    if ((s = norm2_planes(c, r, &n_ext)) || (s = norm2_planes(c, r2, &n_l)) || (s = dot_dev(c, r, r2, &x1)) ||
+    double n_l = 0, x1 = 0, x2 = 0;
+    if ((s = norm2_planes(c, r2, &n_l)) || (s = dot_dev(c, r, r2, &x1)) ||
         (s = dot_dev(c, r + c->n, r2 + c->n, &x2)))
         return s;
     const double rx = x1 + x2;

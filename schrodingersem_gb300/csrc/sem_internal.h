@@ -190,6 +190,7 @@ struct LearnArgs {
     double* r;            // RESID out / FEATURES in: residual (continuous), 2 planes
     const double* V;      // FEATURES: potential
     double alpha;         // FEATURES: stage coefficient
+    double rho_floor;     // FEATURES: lower bound of the per-element residual scale
     void* x;              // FEATURES out: BF16 rows [E][4 N^2]
     float* sigma;         // FEATURES out / TARGETS, CORRECT in: per-element scale
     const double* z;      // TARGETS: converged stage solution

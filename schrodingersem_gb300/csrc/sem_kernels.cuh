@@ -243,14 +243,16 @@ __global__ void k_resid_cont(DevMesh m, const double* __restrict__ b, const doub
 }
 
 // One warp per element.  rho_e = RMS of the residual over the element's
-// nodes (both planes), mbar_e = mean lumped mass w_i w_j J of the element;
+// nodes (both planes), at least rho_floor (elements the residual has not
+// reached get small features and targets instead of scaled round-off),
+// mbar_e = mean lumped mass w_i w_j J of the element;
 // features (BF16, row e):
 //   [r_re / rho, r_im / rho, alpha V, (w_i w_j J) / alpha]   (4 N^2 values)
 // and the element's solution scale sigma_e = rho_e / mbar_e (the size of
 // M^-1 r, the error a mass-dominated residual of size rho points to)
 template <int N>
 __global__ void k_features(DevMesh m, const double* __restrict__ r, const double* __restrict__ V, double alpha,
-                           __nv_bfloat16* __restrict__ x, float* __restrict__ sigma)
+                           double rho_floor, __nv_bfloat16* __restrict__ x, float* __restrict__ sigma)
 {
     constexpr int NN = N * N;
     const long long n = m.n;
@@ -269,7 +271,7 @@ __global__ void k_features(DevMesh m, const double* __restrict__ r, const double
         s += __shfl_xor_sync(0xffffffffu, s, o);
         ms += __shfl_xor_sync(0xffffffffu, ms, o);
     }
-    const double rho = sqrt(s / (2.0 * NN)) + 1e-300;
+    const double rho = fmax(sqrt(s / (2.0 * NN)), rho_floor);
     const double inv = 1.0 / rho;
     __nv_bfloat16* row = x + (long long)e * 4 * NN;
     for (int k = lane; k < NN; k += 32) {
@@ -485,7 +487,8 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
     switch (a.what) {
         case LEARN_RESID: k_resid_cont<N><<<grid, 256, 0, st>>>(m, a.b, a.Y, a.r); break;
         case LEARN_FEATURES:
-            k_features<N><<<(m.E + 7) / 8, 256, 0, st>>>(m, a.r, a.V, a.alpha, (__nv_bfloat16*)a.x, a.sigma);
+            k_features<N><<<(m.E + 7) / 8, 256, 0, st>>>(m, a.r, a.V, a.alpha, a.rho_floor, (__nv_bfloat16*)a.x,
+                                                           a.sigma);
             break;
         case LEARN_TARGETS: k_targets<N><<<grid, 256, 0, st>>>(m, a.z, a.zg, a.sigma, a.t); break;
         case LEARN_CORRECT: k_correct<N><<<grid, 256, 0, st>>>(m, a.zg, a.sigma, a.delta, a.zo); break;

@@ -518,6 +518,10 @@ extern "C" int sem_learner_fit(sem_learner* L, const void* X, const float* T, lo
             double loss = 0.0;
             status = sem_learner_train_step(L, B, Xb, Tb, lr, &loss);
             if (status) break;
+            if (!std::isfinite(loss)) {
+                status = lfail(L, SEM_ERR_ARG, "non-finite training loss (inputs, targets or learning rate)");
+                break;
+            }
             sum += loss;
             ++nb;
         }
