@@ -283,18 +283,18 @@ FORMS = {
                                        "extrapolated linearly from the last two steps (test relative to |b|)"),
     "mixed_diag_extrap": ("mixed", 1e-4, 1, "FP32-inner MINRES with diagonal preconditioner in FP64 iterative "
                                             "refinement, extrapolated stage guess (test relative to |b|)"),
-    "mixed_fdm": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation |A|^-1 "
+    "mixed_fdm": ("mixed", 3e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation |A|^-1 "
                                     "preconditioner in FP64 iterative refinement, zero stage guess"),
-    "mixed_fdm_extrap": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+    "mixed_fdm_extrap": ("mixed", 3e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
                                            "preconditioner in FP64 iterative refinement, extrapolated stage "
                                            "guess (test relative to |b|)"),
-    "mixed_fdm_learned": ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+    "mixed_fdm_learned": ("mixed", 3e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
                                             "preconditioner in FP64 iterative refinement, stage guess = "
                                             "linear extrapolation corrected by the BF16 network (trained on the "
                                             "GPU on stage solves of other initial packets), residual-minimising "
                                             "step"),
 }
-FORMS["mixed_fdm_extrap2"] = ("mixed", 1e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
+FORMS["mixed_fdm_extrap2"] = ("mixed", 3e-4, 2, "FP32-inner MINRES with the element fast-diagonalisation "
                                                 "preconditioner in FP64 iterative refinement, stage guess "
                                                 "extrapolated quadratically from the last three steps")
 GUESS = {"mixed_extrap": 1, "mixed_diag_extrap": 1, "mixed_fdm_extrap": 1, "mixed_fdm_extrap2": 1,

@@ -203,7 +203,7 @@ extern "C" int sem_batch_create(sem_batch** out, int n_inst, const int* p, const
     float* pool32 = nullptr;
     double* vpool = nullptr;
     SolveOut* outs = nullptr;
-    const long long per64 = 12, per32 = 23;  // values per local node
+    const long long per64 = 12, per32 = 25;  // values per local node
     if ((s = balloc(b, (void**)&pool64, sizeof(double) * per64 * tot)) ||
         (s = balloc(b, (void**)&pool32, sizeof(float) * per32 * tot)) ||
         (s = balloc(b, (void**)&vpool, sizeof(double) * tot)) ||
@@ -247,6 +247,7 @@ extern "C" int sem_batch_create(sem_batch** out, int n_inst, const int* p, const
         for (int q = 0; q < 3; ++q) I.w.W[q] = t32(2 * v);
         for (int q = 0; q < 2; ++q) I.w.Y[q] = t32(2 * v);
         for (int q = 0; q < 2; ++q) I.w.Z[q] = t32(2 * v);
+        I.w.Y3 = t32(2 * v);
         I.x32 = t32(2 * v);
         I.pot32 = t32(v);
         I.V = vpool + ov;

@@ -1201,7 +1201,9 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
         if ((s = wsget(c, "k32_AZ", v, &w.AZ)) || (s = wsget(c, "k32_Y3", v, &w.Y3))) return s;
     }
     if (c->precond == SEM_PRECOND_FDM && op == OP_RES) {
-        if ((s = wsget(c, "k32_Z0", v, &w.Z[0])) || (s = wsget(c, "k32_Z1", v, &w.Z[1]))) return s;
+        if ((s = wsget(c, "k32_Z0", v, &w.Z[0])) || (s = wsget(c, "k32_Z1", v, &w.Z[1])) ||
+            (s = wsget(c, "k32_Y3", v, &w.Y3)))
+            return s;
         mx.fdm = 1;
         mx.fused = 0;
     } else if (c->precond) {

@@ -350,6 +350,26 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                 iw2 = iw;
                 iw = tmp;
             }
+            if constexpr (PRE == 2) {
+                // local solves of y itself, ahead of alpha: the preconditioner
+                // is linear, so P^-1 y5 = P^-1 y - (alpha/beta) z_it is formed
+                // in Phase A without a barrier of its own (y of this block's
+                // elements is complete after the block barrier)
+                __syncthreads();
+                for (int e0 = eb; e0 < ee; e0 += kmax)
+                    fdm_range<N, T, NC>(
+                        sm, kmax, fS, fL, m, alpha, e0, min(kmax, ee - e0),
+                        [&](int e, int i, int j, long long flat, T* u) {
+                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) u[c] = wt * L[iy][c * n + flat];
+                        },
+                        [&](int e, int i, int j, long long flat, const T* z) {
+                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
+#pragma unroll
+                            for (int c = 0; c < NC; ++c) w.Y3[c * n + flat] = wt * z[c];
+                        });
+            }
             double S1 = 0.0, dummy = 0.0;
             grid_sum2_t<T>(s1, T(0), w.partials, slot, gs, tmo, red, ok, S1, dummy);
             slot ^= 1;
@@ -365,32 +385,8 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
             T ss = T(0);
             T* Ynext = w.Y[it & 1];
             if constexpr (PRE == 2) {
-                // y5 and its weighted local solves (into Y[it-1], read in
-                // Phase B above); after the barrier z = DSS -> Z[it & 1]
-                T* Zl = w.Y[(it - 1) & 1];
-                for (int e0 = eb; e0 < ee; e0 += kmax)
-                    fdm_range_post<N, T, NC, true>(
-                        sm, kmax, fS, fL, m, alpha, e0, min(kmax, ee - e0),
-                        [&](int e, int i, int j, long long flat, T* u, T* aux) {
-                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
-#pragma unroll
-                            for (int c = 0; c < NC; ++c) {
-                                const long long q = c * n + flat;
-                                const T y5 = L[iy][q] - c2 * L[ir2][q];
-                                aux[c] = y5;
-                                u[c] = wt * y5;
-                            }
-                        },
-                        [&](int, int, int, long long flat, const T*, const T* aux) {
-#pragma unroll
-                            for (int c = 0; c < NC; ++c) L[iy][c * n + flat] = aux[c];
-                        },
-                        [&](int e, int i, int j, long long flat, const T* z) {
-                            const T wt = nn_weight<N, T>(m, node_info<N>(m, e, i, j), e);
-#pragma unroll
-                            for (int c = 0; c < NC; ++c) Zl[c * n + flat] = wt * z[c];
-                        });
-                if (!grid_barrier(gs, tmo)) return false;
+                // z_{it+1} = DSS(local solves of y) - c2 z_it, y5 = y - c2 r2
+                const T* Zc = w.Z[(it - 1) & 1];
                 T* Zn = w.Z[it & 1];
                 for (int e0 = eb; e0 < ee; e0 += kmax)
                     apply_range_post<N, T, OP, true>(
@@ -400,14 +396,15 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
                                 const long long q = c * n + flat;
-                                u[c] = dss_value<N, T, DSS_CONT>(m, Zl + c * n, ni, e, flat);
-                                aux[c] = L[iy][q];
+                                u[c] = dss_value<N, T, DSS_CONT>(m, w.Y3 + c * n, ni, e, flat) - c2 * Zc[q];
+                                aux[c] = L[iy][q] - c2 * L[ir2][q];
                             }
                         },
                         [&](int e, int i, int j, long long flat, const T* u, const T* aux) {
                             const bool own = ni_owner(node_info<N>(m, e, i, j));
 #pragma unroll
                             for (int c = 0; c < NC; ++c) {
+                                L[iy][c * n + flat] = aux[c];
                                 Zn[c * n + flat] = u[c];
                                 if (own) ss = fma(aux[c], u[c], ss);
                             }
