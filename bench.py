@@ -243,12 +243,24 @@ def batch_cpu_baseline(n_instances, sample=16, steps=2):
                       f"measured seconds per node-step)", "all_converged": all(r[1] for r in res)}
 
 
-def apply_gbs(ctx, torch, reps=20):
-    """standalone Res apply (element kernel + assembly) with L2 flushed before
-    each apply: algorithmic bytes n_loc * s * 9 words per apply"""
+APPLY_NEL = 559  # 559^2 elements at p = 8: 4473^2 = 20.0 M global nodes
+FP64_PEAK_TFLOPS = 1.19  # FMA-chain probe of the FP64 pipe on this GB300
+
+
+def apply_gbs(S, torch, reps=20):
+    """standalone Res apply (element kernel + assembly into the masked
+    format) on 559x559 jittered quads over [-12,12]^2 at p = 8 (20.0 M global
+    nodes, 25.3 M element-local nodes per plane, above L2), L2 flushed before
+    each apply.  Algorithmic bytes n_loc * s * 9 (psi 2 planes, out 2,
+    g11 g12 g22 mass, V) and flops n_loc * (16 N + 23) per apply."""
+    from schrodingersem_gb300.meshgen import structured_quads
+    co, el = structured_quads(APPLY_NEL, box=(-12.0, 12.0, -12.0, 12.0), jitter=0.1, seed=1)
+    ctx = S.Context(P, coords=co, elements=el)
     n = ctx.n
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
-    out = {}
+    out = {"workload": f"{APPLY_NEL}x{APPLY_NEL} jittered quads on [-12,12]^2, p={P} "
+                       f"({(APPLY_NEL * P + 1) ** 2:,} global nodes, {n:,} element-local nodes per plane)",
+           "l2": "flushed before every apply (256 MiB write)", "reps": reps}
     for prec, dt, s in (("fp64", torch.float64, 8), ("fp32", torch.float32, 4)):
         g = torch.Generator(device="cuda").manual_seed(0)
         q = [torch.randn(ctx.shape, dtype=dt, device="cuda", generator=g) for _ in range(3)]
@@ -268,7 +280,17 @@ def apply_gbs(ctx, torch, reps=20):
             tot += e0.elapsed_time(e1)
         ms = tot / reps
         bytes_ = n * s * 9
-        out[prec] = {"ms": ms, "gbs": bytes_ / ms / 1e6, "bytes": bytes_}
+        flops = n * (16 * ctx.N + 23)
+        out[prec] = {"ms": ms, "gbs": bytes_ / ms / 1e6, "bytes": bytes_,
+                     "tflops": flops / ms / 1e9, "flops": flops}
+        del q, yr, yi
+    out["fp32"]["bound"] = "hbm"
+    out["fp64"]["bound"] = "fp64"
+    out["fp64"]["frac_fp64"] = out["fp64"]["tflops"] / FP64_PEAK_TFLOPS
+    out["fp64"]["fp64_peak_tflops"] = FP64_PEAK_TFLOPS
+    ctx.close()
+    del flush
+    torch.cuda.empty_cache()
     return out
 
 
@@ -507,7 +529,7 @@ def run_ours(args):
     nbytes = ctx.n * 8
     if rank != 0:
         return
-    app = apply_gbs(ctx, torch)
+    app = apply_gbs(S, torch)
     # algorithmic bytes of the dominant kernel (the persistent solver):
     # per Krylov iteration one Res apply (9 words/node) + 13 two-plane vector
     # words; per FP64 refinement sweep one FP64 residual (apply + 5 words)
@@ -554,11 +576,13 @@ def run_ours(args):
                      "algorithmic_bytes": alg_bytes, "fp64_iterations": H["it64"], "fp32_iterations": H["it32"],
                      "kernel_ms": H["solver_ms"], "peak_source": peak_src,
                      "fp64_pipe": ({"achieved_tflops": flops64 * H["it64"] / (H["solver_ms"] / 1e3) / 1e12,
-                                    "peak_tflops": 1.19, "peak_source": "FMA-chain probe on this pool's GB300"}
+                                    "peak_tflops": FP64_PEAK_TFLOPS, "peak_source": "FMA-chain probe on a GB300"}
                                    if prec == "fp64" and H["solver_ms"] > 0 else None)},
-        "apply": {"fp64_gbs": app["fp64"]["gbs"], "fp32_gbs": app["fp32"]["gbs"],
-                  "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak, "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
-                  "bytes_fp64": app["fp64"]["bytes"], "note": "n_loc*s*9 words, L2 flushed before each apply"},
+        "apply": {"fp32_gbs": app["fp32"]["gbs"], "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
+                  "fp64_gbs": app["fp64"]["gbs"], "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak,
+                  "fp64_tflops": app["fp64"]["tflops"], "fp64_frac_fp64_pipe": app["fp64"]["frac_fp64"],
+                  "detail": app, "note": "n_loc*s*9 algorithmic words and n_loc*(16N+23) flops per apply; "
+                                         "the FP64 apply is bound by GB300's FP64 pipe, the FP32 apply by HBM"},
         "cpu_baseline": cpu,
         "batch": batch,
         "e2e": {"value": e2e_s, "unit": "s/step", "h2d_bytes_per_step": 3 * nbytes,

@@ -156,8 +156,8 @@ struct DMat {
 //   P3  row l:    lap(l,:) = lap1(l,:) + f2(l,:) D, then the mass/potential
 //       epilogue of the operator                -> W2
 // and W2 is written out with one bulk store per component.  Every
-// accumulation runs over k in ascending order as in apply_range, so both
-// kernels give the same bits.
+// accumulation runs over k in ascending order as in apply_chunk (the
+// one-pass kernel), so both kernels give the same bits.
 template <int N, typename T, int OP, bool GATHER>
 __global__ void __launch_bounds__(bulk_tpb<T, OP>())
     k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,

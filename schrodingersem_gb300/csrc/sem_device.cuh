@@ -125,23 +125,40 @@ __device__ __forceinline__ T ldcg(const T* p) { return __ldcg(p); }
 // assembled value at a node (global_sum.hpp:13-63 + mask.hpp:16-28 by mode).
 // Values of other elements are read with ld.cg: inside the persistent
 // kernels they were written by other blocks in the previous phase.
+// The index tables of a node are read before its flags are tested, so a side
+// copy costs two dependent loads (tables, other copy) and a corner copy two
+// (its copy list, the copies).
 template <int N, typename T, int MODE>
 __device__ __forceinline__ T dss_value(const DevMesh& m, const T* Y, const NodeInfo& ni, int e,
                                        long long flat)
 {
     const T own = ldcg(Y + flat);
     if (ni.kind == 0) return own;
+    if (ni.kind == 1) {
+        const int sb = __ldg(m.side_base + 4 * e + ni.sc), ss = __ldg(m.side_step + 4 * e + ni.sc);
+        if (ni_boundary(ni)) return MODE == DSS_SUM ? own : T(0);
+        if (MODE == DSS_MASK && !ni_owner(ni)) return T(0);
+        return own + ldcg(Y + ((long long)sb + (long long)ni.k * ss));  // owner + other in either copy: same bits
+    }
+    const int* cl = m.corner_nb + (size_t)(4 * e + ni.sc) * CORNER_NB_MAX;
+    int q[CORNER_NB_MAX];
+#pragma unroll
+    for (int k = 0; k < CORNER_NB_MAX; ++k) q[k] = __ldg(cl + k);
     if (ni_boundary(ni)) return MODE == DSS_SUM ? own : T(0);
     if (MODE == DSS_MASK && !ni_owner(ni)) return T(0);
-    if (ni.kind == 1) {
-        const long long nf = (long long)__ldg(m.side_base + 4 * e + ni.sc) +
-                             (long long)ni.k * __ldg(m.side_step + 4 * e + ni.sc);
-        return own + ldcg(Y + nf);  // owner + other in either copy: commutative, same bits
-    }
-    const int node = __ldg(m.corner_node + 4 * e + ni.sc);
-    const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
     T s = T(0);  // csum = 0, then += in connected_elements order (global_sum.hpp:56-59)
-    for (int q = q0; q < q1; ++q) s += ldcg(Y + __ldg(m.node_flat + q));
+    if (q[0] == -2) {  // more copies than the table holds
+        const int node = __ldg(m.corner_node + 4 * e + ni.sc);
+        const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
+        for (int k = q0; k < q1; ++k) s += ldcg(Y + __ldg(m.node_flat + k));
+        return s;
+    }
+    T v[CORNER_NB_MAX];
+#pragma unroll
+    for (int k = 0; k < CORNER_NB_MAX; ++k) v[k] = q[k] >= 0 ? ldcg(Y + q[k]) : T(0);
+#pragma unroll
+    for (int k = 0; k < CORNER_NB_MAX; ++k)
+        if (q[k] >= 0) s += v[k];
     return s;
 }
 
@@ -435,10 +452,10 @@ template <int N, typename T>
 __device__ __forceinline__ T nn_weight(const DevMesh& m, const NodeInfo& ni, int e)
 {
     if (ni.kind == 0) return T(1);
+    const int c4 = ni.kind == 2 ? __ldg(m.corner_cnt4 + e) : 0;
     if (ni_boundary(ni)) return T(0);
     if (ni.kind == 1) return T(0.5);
-    const int node = __ldg(m.corner_node + 4 * e + ni.sc);
-    return T(1) / T(__ldg(m.node_ptr + node + 1) - __ldg(m.node_ptr + node));
+    return T(1) / T((c4 >> (8 * ni.sc)) & 255);
 }
 
 template <typename T>

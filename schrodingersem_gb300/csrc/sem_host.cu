@@ -478,6 +478,21 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             if (node_bnd[node]) fl[e] |= (4096 << cc);
         }
     for (int k = 0; k < n_nodes; ++k) c->n_bnd_nodes += node_bnd[k];
+    // corner copies in CSR order per element corner (the gathers read them
+    // with one dependent load instead of three)
+    std::vector<int> corner_nb((size_t)n_el * 4 * CORNER_NB_MAX, -1), corner_cnt4(n_el, 0);
+    for (int e = 0; e < n_el; ++e)
+        for (int cc = 0; cc < 4; ++cc) {
+            const int node = cnode[4 * e + cc];
+            const int q0 = nptr[node], cnt = nptr[node + 1] - q0;
+            if (cnt > 255) return fail(SEM_ERR_MESH, "a corner node is shared by more than 255 elements");
+            corner_cnt4[e] |= cnt << (8 * cc);
+            int* dst = &corner_nb[((size_t)e * 4 + cc) * CORNER_NB_MAX];
+            if (cnt > CORNER_NB_MAX)
+                dst[0] = -2;
+            else
+                for (int q = 0; q < cnt; ++q) dst[q] = nflat[q0 + q];
+        }
     // ring tables of the in-place assembly and the pipelined apply's gather
     const int R = 4 * (N - 1);
     std::vector<int> ring_src((size_t)n_el * R, -1), bnd_flat;
@@ -651,6 +666,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, fS, &d.fdmS64)) || (s = upload(c, tof(fS), &d.fdmS32)) ||
         (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)) ||
         (s = upload(c, ring_src, &d.ring_src)) || (s = upload(c, edge_pairs, &d.edge_pairs)) ||
+        (s = upload(c, corner_nb, &d.corner_nb)) || (s = upload(c, corner_cnt4, &d.corner_cnt4)) ||
         (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)))
         return s;
     d.n_pairs = (long long)edge_pairs.size();

@@ -10,6 +10,7 @@ namespace semgb {
 
 constexpr int MIN_N = 2;   // p = 1
 constexpr int MAX_N = 17;  // p = 16
+constexpr int CORNER_NB_MAX = 8;  // copies per corner node held in DevMesh::corner_nb
 
 // Element-local operator kinds (the closures of the reference's drivers).
 enum OpKind : int {
@@ -68,6 +69,12 @@ struct DevMesh {
     // excluded); bnd_flat = copies on boundary sides (corners excluded);
     // node_bnd = corner node on the boundary
     const int* ring_src = nullptr;
+    // corner copies of every element corner (4 per element, CORNER_NB_MAX
+    // entries each): the flat indices of all copies of the corner node in
+    // CSR order, -1 padded, first entry -2 when the node has more copies;
+    // corner_cnt4[e] packs the four corners' copy counts, 8 bits each
+    const int* corner_nb = nullptr;
+    const int* corner_cnt4 = nullptr;
     const int2* edge_pairs = nullptr;
     const int* bnd_flat = nullptr;
     const char* node_bnd = nullptr;

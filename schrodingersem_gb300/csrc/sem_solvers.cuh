@@ -94,7 +94,7 @@ __device__ __forceinline__ void grid_sum2_t(T v0, T v1, double* partials, int sl
 // MINRES scalar state (minres.hpp:28-40, 65-84), shared memory, thread 0 only
 template <typename T>
 struct MinresScal {
-    double bnorm, beta, beta_old, phibar, cs, sn, dbar, eps;
+    double bnorm, beta, beta_old, phibar, cs, sn, dbar, eps, inv_beta;
     double pg, peps, pdelta, pphi, pinvb, alpha_i;
     int pending, conv, stop;
     // coefficients of the next vector pass, in T
@@ -106,6 +106,7 @@ __device__ __forceinline__ void scal_init(MinresScal<T>& sc, double bnorm, doubl
 {
     sc.bnorm = bnorm;
     sc.beta = beta1;
+    sc.inv_beta = 1.0 / beta1;
     sc.beta_old = 0.0;
     sc.phibar = beta1;
     sc.cs = -1.0;
@@ -157,6 +158,52 @@ __device__ __forceinline__ void scal_givens(MinresScal<T>& sc, double alpha_i, d
     sc.beta_old = sc.beta;
     sc.beta = beta_new;
     sc.conv = sc.phibar < tol_rel * sc.bnorm + tol_abs;  // minres.hpp:92
+}
+
+// scal_givens + scal_publish of one iteration (it_next >= 2) for the FP32
+// inner solver, with the square roots and reciprocals taken from two FP64
+// reciprocal square roots: on one thread, GB300's FP64 division and square
+// root are long dependent sequences on the critical path of every iteration.
+template <typename T>
+__device__ __forceinline__ void scal_step_rsqrt(MinresScal<T>& sc, double alpha_i, double bnew2, double eps_mach,
+                                                double tol_rel, double tol_abs)
+{
+    const double inv_beta_new = bnew2 > 0.0 ? rsqrt(bnew2) : 1.0 / bnew2;
+    const double beta_new = bnew2 > 0.0 ? bnew2 * inv_beta_new : 0.0;
+    const double eps_old = sc.eps;
+    const double delta = sc.cs * sc.dbar + sc.sn * alpha_i;
+    const double gbar = sc.sn * sc.dbar - sc.cs * alpha_i;
+    sc.eps = sc.sn * beta_new;
+    sc.dbar = -sc.cs * beta_new;
+    const double g2 = gbar * gbar + beta_new * beta_new;
+    double ig = rsqrt(g2), gamma = g2 * ig;
+    if (!(gamma >= eps_mach)) {
+        gamma = eps_mach;
+        ig = 1.0 / eps_mach;
+    }
+    sc.cs = gbar * ig;
+    sc.sn = beta_new * ig;
+    const double phi = sc.cs * sc.phibar;
+    sc.phibar *= sc.sn;
+    sc.pending = 1;
+    sc.pg = ig;
+    sc.peps = eps_old;
+    sc.pdelta = delta;
+    sc.pphi = phi;
+    sc.pinvb = sc.inv_beta;
+    const double c1 = beta_new * sc.inv_beta;
+    sc.beta_old = sc.beta;
+    sc.beta = beta_new;
+    sc.inv_beta = inv_beta_new;
+    sc.conv = sc.phibar < tol_rel * sc.bnorm + tol_abs;  // minres.hpp:92
+    sc.inv_b = (T)inv_beta_new;
+    sc.c1 = (T)c1;
+    sc.cq = T(0);
+    sc.tpg = (T)sc.pg;
+    sc.tpeps = (T)sc.peps;
+    sc.tpdelta = (T)sc.pdelta;
+    sc.tpphi = (T)sc.pphi;
+    sc.tpinvb = (T)sc.pinvb;
 }
 
 // include/minres.hpp:19-107 inside a cooperative kernel.  Lanczos vectors
@@ -445,9 +492,14 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
                 iy = tmp;
             }
             if (threadIdx.x == 0) {
-                scal_givens(sc, sc.alpha_i, sqrt(bnew2), eps_mach, tol_rel, tol_abs);
-                sc.stop = sc.conv || it == maxit;
-                scal_publish(sc, it + 1, 0.0);
+                if constexpr (sizeof(T) == 4) {
+                    scal_step_rsqrt(sc, sc.alpha_i, bnew2, eps_mach, tol_rel, tol_abs);
+                    sc.stop = sc.conv || it == maxit;
+                } else {
+                    scal_givens(sc, sc.alpha_i, sqrt(bnew2), eps_mach, tol_rel, tol_abs);
+                    sc.stop = sc.conv || it == maxit;
+                    scal_publish(sc, it + 1, 0.0);
+                }
             }
             __syncthreads();
             if (sc.stop) break;
