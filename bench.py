@@ -39,6 +39,11 @@ WORKLOAD = ("Schroedinger SDIRK4-3 time step, 64x64 jittered quads on [-8,8]^2 (
             "MINRES tol 1e-10")
 DT, TOL, P, NEL = 1e-2, 1e-10, 8, 64
 ORACLE_TOL = 1e-13  # MINRES tolerance of the FP64 accuracy reference run
+# DRAM bytes (read + write) per launch of the element-preconditioned FP32
+# solver kernel on this workload: mean of three launches of the timed steps
+# captured with ncu (dram__bytes_read.sum + dram__bytes_write.sum).  The
+# solver's working set stays in L2, so this is far below the algorithmic bytes.
+SOLVER_DRAM_BYTES_PER_LAUNCH = 90.8e6
 
 
 def workload_inputs():
@@ -404,9 +409,11 @@ def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, clocks=None):
     for _ in range(steps):
         flush_l2(flush)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.nvtx.range_push(f"timed_{form}")  # profilers can select the timed steps of a form
         e0.record(st)
         one_step(dre, dim, dV)
         e1.record(st)
+        torch.cuda.nvtx.range_pop()
         torch.cuda.synchronize()
         times.append(e0.elapsed_time(e1))
         sts = ctx.stats()
@@ -529,7 +536,7 @@ def run_ours(args):
     nbytes = ctx.n * 8
     if rank != 0:
         return
-    app = apply_gbs(S, torch)
+    app = apply_gbs(S, torch) if not args.no_apply else None
     # algorithmic bytes of the dominant kernel (the persistent solver):
     # per Krylov iteration one Res apply (9 words/node) + 13 two-plane vector
     # words; per FP64 refinement sweep one FP64 residual (apply + 5 words)
@@ -553,8 +560,8 @@ def run_ours(args):
         if not args.no_cpu else None
     # the batched-ensemble workload (1,024 seeded instances, BDF2)
     from schrodingersem_gb300.batch_bench import run_batch
-    batch = run_batch(1024, steps=args.batch_steps, warmup=2)
-    if not args.no_cpu:
+    batch = run_batch(1024, steps=args.batch_steps, warmup=2) if args.batch_steps > 0 else None
+    if batch and not args.no_cpu:
         batch["cpu_baseline"] = batch_cpu_baseline(1024)
         batch["speedup_vs_cpu"] = batch["value"] / batch["cpu_baseline"]["value"]
     flops64 = n * (2 * (8 * ctx.N + 14) + 6 + 2 * 13)
@@ -571,18 +578,23 @@ def run_ours(args):
         "fastest_form": {"form": best, "s_per_step": res[best]["ms"] / 1e3,
                          "speedup_vs_plain_fp64": (res["fp64"]["ms"] / res[best]["ms"]) if "fp64" in res else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": (achieved / hbm_peak) if achieved else None, "traffic": None,
+                     "frac": (achieved / hbm_peak) if achieved else None,
+                     "traffic": SOLVER_DRAM_BYTES_PER_LAUNCH if FORMS[head][2] == 2 and prec == "mixed" else None,
+                     "traffic_unit": "bytes per launch (ncu capture of the timed steps)",
+                     "algorithmic_bytes_per_launch": alg_bytes / (3 * args.steps),
+                     "launches": 3 * args.steps,
                      "kernel": kern + " (persistent cooperative solver)",
                      "algorithmic_bytes": alg_bytes, "fp64_iterations": H["it64"], "fp32_iterations": H["it32"],
                      "kernel_ms": H["solver_ms"], "peak_source": peak_src,
                      "fp64_pipe": ({"achieved_tflops": flops64 * H["it64"] / (H["solver_ms"] / 1e3) / 1e12,
                                     "peak_tflops": FP64_PEAK_TFLOPS, "peak_source": "FMA-chain probe on a GB300"}
                                    if prec == "fp64" and H["solver_ms"] > 0 else None)},
-        "apply": {"fp32_gbs": app["fp32"]["gbs"], "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
-                  "fp64_gbs": app["fp64"]["gbs"], "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak,
-                  "fp64_tflops": app["fp64"]["tflops"], "fp64_frac_fp64_pipe": app["fp64"]["frac_fp64"],
-                  "detail": app, "note": "n_loc*s*9 algorithmic words and n_loc*(16N+23) flops per apply; "
-                                         "the FP64 apply is bound by GB300's FP64 pipe, the FP32 apply by HBM"},
+        "apply": ({"fp32_gbs": app["fp32"]["gbs"], "fp32_frac_hbm": app["fp32"]["gbs"] / hbm_peak,
+                   "fp64_gbs": app["fp64"]["gbs"], "fp64_frac_hbm": app["fp64"]["gbs"] / hbm_peak,
+                   "fp64_tflops": app["fp64"]["tflops"], "fp64_frac_fp64_pipe": app["fp64"]["frac_fp64"],
+                   "detail": app, "note": "n_loc*s*9 algorithmic words and n_loc*(16N+23) flops per apply; "
+                                          "the FP64 apply is bound by GB300's FP64 pipe, the FP32 apply by HBM"}
+                  if app else None),
         "cpu_baseline": cpu,
         "batch": batch,
         "e2e": {"value": e2e_s, "unit": "s/step", "h2d_bytes_per_step": 3 * nbytes,
@@ -602,7 +614,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
-    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched-ensemble workload")
+    ap.add_argument("--batch-steps", type=int, default=10,
+                    help="timed steps of the batched-ensemble workload (0: skip it)")
+    ap.add_argument("--no-apply", action="store_true", help="skip the 20M-node operator-apply measurement")
     ap.add_argument("--forms", default="fp64,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_extrap2,mixed_fdm_learned",
                     help="solver forms to time (comma list)")
     args = ap.parse_args()
