@@ -161,7 +161,7 @@ struct DMat {
 template <int N, typename T, int OP, bool GATHER>
 __global__ void __launch_bounds__(bulk_tpb<T, OP>())
     k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
-                 const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk,
+                 const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk, int pair_asm,
                  long long timeout_ns)
 {
     constexpr int NN = N * N;
@@ -260,7 +260,26 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
             for (int c = 0; c < NC; ++c) st[c * BN + le * NN + ii + jj * N] = gval[q][c];
         }
     };
+    // side pairs with both copies in the batch (pair_asm): owner += other,
+    // other = 0 in the staged result, before it is stored; the entries of the
+    // next batch are loaded while the current one computes
+    constexpr int PQ = (2 * K * (N - 2) + TPB - 1) / TPB > 0 ? (2 * K * (N - 2) + TPB - 1) / TPB : 1;
+    int ppair[PQ];
+    auto pair_fetch = [&](long long bb) {
+        int p0 = 0, p1 = 0;
+        if (pair_asm && bb < nbatch) {
+            p0 = __ldg(m.bulk_pair_ptr + bb);
+            p1 = __ldg(m.bulk_pair_ptr + bb + 1);
+            if (threadIdx.x == 0 && p1 - p0 > PQ * TPB) atomicExch(m.dev_err, 2);  // cannot happen: <= 2K(N-2)
+        }
+#pragma unroll
+        for (int q = 0; q < PQ; ++q) {
+            const int t = p0 + threadIdx.x + q * TPB;
+            ppair[q] = t < p1 ? __ldg(m.bulk_pairs + t) : -1;
+        }
+    };
     if (GATHER) gather_fetch(blockIdx.x);
+    pair_fetch(blockIdx.x);
     int it = 0;
     for (long long b = blockIdx.x; b < nbatch; b += G, ++it) {
         const int s = it % S;
@@ -407,6 +426,20 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
                     W1[c * BN + q] = o;
                 }
             }
+            if (pair_asm) {
+                __syncthreads();
+#pragma unroll
+                for (int q = 0; q < PQ; ++q) {
+                    if (ppair[q] < 0) continue;
+                    const int po = ppair[q] >> 16, px = ppair[q] & 0xffff;
+#pragma unroll
+                    for (int cc = 0; cc < NC; ++cc) {
+                        W1[cc * BN + po] = W1[cc * BN + po] + W1[cc * BN + px];  // owner + other, as k_ring
+                        W1[cc * BN + px] = T(0);
+                    }
+                }
+                pair_fetch(b + G);
+            }
             fence_proxy_async_smem();
             __syncthreads();
             if (store_bulk && b < nfull) {
@@ -434,7 +467,7 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
 // grid of k_apply_bulk for one instantiation (occupancy queried once per process)
 template <int N, typename T, int OP, bool GATHER>
 cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
-                                long long timeout_ns, cudaStream_t st)
+                                bool pair_asm, long long timeout_ns, cudaStream_t st)
 {
     static int blocks_per_sm = -1, sms = 0;
     constexpr size_t smem = bulk_smem_bytes<N, T, OP>();
@@ -459,8 +492,11 @@ cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T
     const long long nbatch = (m.E + K - 1) / K;
     const int grid = (int)std::min<long long>(nbatch, (long long)sms * blocks_per_sm);
     const int store_bulk = (((uintptr_t)y0 | (uintptr_t)(y1 ? y1 : y0)) & 15u) == 0;
+    // batch-local pair tables exist for the FP32 Res batching only
+    const int pa = (pair_asm && OP == OP_RES && sizeof(T) == 4 && m.bulk_K == K && m.bulk_pair_ptr) ? 1 : 0;
+    if (pair_asm && !pa) return cudaErrorInvalidValue;
     k_apply_bulk<N, T, OP, GATHER>
-        <<<grid, bulk_tpb<T, OP>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, timeout_ns);
+        <<<grid, bulk_tpb<T, OP>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
     return cudaGetLastError();
 }
 

@@ -15,6 +15,7 @@
 
 #include "sem_gb300.h"
 #include "sem_internal.h"
+#include "sem_apply_bulk.cuh"
 
 using namespace semgb;
 
@@ -538,6 +539,33 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         }
     }
     c->dof = (long long)n_nodes + (long long)c->n_edges * (N - 2) + (long long)n_el * (N - 2) * (N - 2);
+    // side pairs inside one batch of the pipelined FP32 apply go last in
+    // edge_pairs and into per-batch tables of batch-local offsets
+    const int bK = bulk_k<float, OP_RES>(N);
+    const long long bN = (long long)bK * NN;
+    const long long nbatch = (n_el + bK - 1) / bK;
+    std::vector<int> bulk_pair_ptr(nbatch + 1, 0), bulk_pairs;
+    long long n_pairs_x = 0;
+    {
+        auto internal = [&](const int2& pr) { return (long long)pr.x / bN == (long long)pr.y / bN; };
+        std::stable_partition(edge_pairs.begin(), edge_pairs.end(), [&](const int2& pr) { return !internal(pr); });
+        for (const int2& pr : edge_pairs) {
+            if (!internal(pr)) {
+                ++n_pairs_x;
+                continue;
+            }
+            bulk_pair_ptr[pr.x / bN + 1]++;
+        }
+        for (long long b = 0; b < nbatch; ++b) bulk_pair_ptr[b + 1] += bulk_pair_ptr[b];
+        bulk_pairs.assign(bulk_pair_ptr[nbatch], 0);
+        std::vector<int> fill(nbatch, 0);
+        for (long long q = n_pairs_x; q < (long long)edge_pairs.size(); ++q) {
+            const int2 pr = edge_pairs[q];
+            const long long b = pr.x / bN;
+            const int o = (int)(pr.x - b * bN), x = (int)(pr.y - b * bN);
+            bulk_pairs[bulk_pair_ptr[b] + fill[b]++] = (o << 16) | x;
+        }
+    }
 
     // metrics, include/Quad.hpp:39-54 (C as the reference writes it unless corrected)
     const bool corrected = (flags & SEM_FLAG_METRIC_CORRECTED) != 0;
@@ -667,9 +695,13 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)) ||
         (s = upload(c, ring_src, &d.ring_src)) || (s = upload(c, edge_pairs, &d.edge_pairs)) ||
         (s = upload(c, corner_nb, &d.corner_nb)) || (s = upload(c, corner_cnt4, &d.corner_cnt4)) ||
+        (s = upload(c, bulk_pair_ptr, &d.bulk_pair_ptr)) ||
+        (!bulk_pairs.empty() && (s = upload(c, bulk_pairs, &d.bulk_pairs))) ||
         (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)))
         return s;
     d.n_pairs = (long long)edge_pairs.size();
+    d.n_pairs_x = n_pairs_x;
+    d.bulk_K = bK;
     d.n_bnd = (long long)bnd_flat.size();
     {
         void* p = nullptr;
@@ -1030,7 +1062,7 @@ static int apply_galerkin(sem_ctx* c, int op, const double* pot, double alpha, c
                                                      c->stream);
         }));
         SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
-            return launch_ring<decltype(nv)::value>(c->dm, false, DSS_MASK, out0, nc == 2 ? out1 : nullptr,
+            return launch_ring<decltype(nv)::value>(c->dm, false, DSS_MASK, out0, nc == 2 ? out1 : nullptr, false,
                                                     c->stream);
         }));
         c->stats.fp64_applies++;
@@ -1097,10 +1129,13 @@ extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, 
     SEM_CHECK_CTX(c);
     if (!V || !qr || !qi || !yr || !yi) return fail(SEM_ERR_ARG, "null field");
     if (apply_direct(c, sizeof(float), V, qr, qi, yr, yi)) {
-        if (c->apply_pipeline && aligned16(V) && aligned16(qr) && aligned16(qi)) {
+        // the pipelined kernel sums the side pairs inside its batches; the
+        // ring pass then assembles the pairs across batches and the corners
+        const bool bulk = c->apply_pipeline && aligned16(V) && aligned16(qr) && aligned16(qi);
+        if (bulk) {
             SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
                 return launch_apply_bulk<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true,
-                                                              timeout_ns(c), c->stream);
+                                                              true, timeout_ns(c), c->stream);
             }));
         } else {
             SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
@@ -1109,7 +1144,7 @@ extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, 
             }));
         }
         SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
-            return launch_ring<decltype(nv)::value>(c->dm, true, DSS_MASK, yr, yi, c->stream);
+            return launch_ring<decltype(nv)::value>(c->dm, true, DSS_MASK, yr, yi, bulk, c->stream);
         }));
         c->stats.fp32_applies++;
         return SEM_OK;

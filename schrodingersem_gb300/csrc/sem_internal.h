@@ -79,6 +79,15 @@ struct DevMesh {
     const int* bnd_flat = nullptr;
     const char* node_bnd = nullptr;
     long long n_pairs = 0, n_bnd = 0;
+    // pipelined FP32 apply: side pairs with both copies inside one batch of
+    // bulk_K elements are summed by the apply kernel itself; edge_pairs lists
+    // the other pairs first (n_pairs_x of them).  bulk_pair_ptr[b] ..
+    // bulk_pair_ptr[b+1] index bulk_pairs of batch b, each packing the batch-
+    // local flat offsets (owner << 16 | other)
+    long long n_pairs_x = 0;
+    int bulk_K = 0;
+    const int* bulk_pair_ptr = nullptr;
+    const int* bulk_pairs = nullptr;
     int* dev_err = nullptr;  // set by a kernel whose bounded wait expired (pipelined apply)
     const double* Dh = nullptr;  // host copy of D, row-major (launchers that pass D by value)
 };
@@ -153,11 +162,13 @@ template <int N>
 cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, double alpha,
                          const void* in0, const void* in1, void* y0, void* y1, bool gather,
                          cudaStream_t st);
-// the same operators through the bulk-copy pipeline (k_apply_bulk); every
-// field pointer 16-byte aligned.  FP64: all operators; FP32: Res.
+// the FP32 Res operator through the bulk-copy pipeline (k_apply_bulk); every
+// field pointer 16-byte aligned (FP64 applies are FP64-pipe bound and use
+// the one-pass kernel).  pair_asm: the kernel also sums the side pairs inside
+// its batches (the masked output then needs launch_ring with cross_only).
 template <int N>
 cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
-                              const void* in1, void* y0, void* y1, bool gather, long long timeout_ns,
+                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, long long timeout_ns,
                               cudaStream_t st);
 template <int N>
 cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
@@ -165,7 +176,10 @@ cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, cons
 // in-place assembly of element-local values touching only element rings
 // (k_ring); equals launch_dss with scale 1 into a separate output
 template <int N>
-cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, cudaStream_t st);
+// cross_only: only the side pairs that cross batches of the pipelined apply
+// (the apply kernel summed the others)
+cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, bool cross_only,
+                        cudaStream_t st);
 template <int N>
 cudaError_t launch_unmask(const DevMesh& m, bool fp32, void* a, cudaStream_t st);
 template <int N>

@@ -60,9 +60,9 @@ __global__ void k_dss(DevMesh m, const T* __restrict__ Y, T* __restrict__ out, T
 // order at corners), so the result equals k_dss<MODE> with scale 1 bit for
 // bit.  Element interiors are final as the apply wrote them.
 template <int N, typename T, int MODE>
-__global__ void k_ring(DevMesh m, T* __restrict__ a0, T* __restrict__ a1)
+__global__ void k_ring(DevMesh m, long long np, T* __restrict__ a0, T* __restrict__ a1)
 {
-    const long long np = m.n_pairs, nb = m.n_bnd;
+    const long long nb = m.n_bnd;
     const long long total = np + nb + m.n_nodes;
     T* planes[2] = {a0, a1};
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -377,14 +377,16 @@ cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, d
 
 template <int N>
 cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
-                              const void* in1, void* y0, void* y1, bool gather, long long timeout_ns,
+                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, long long timeout_ns,
                               cudaStream_t st)
 {
 #define SEM_BULK_CASE(T, OPK)                                                                                 \
     return gather ? launch_apply_bulk_t<N, T, OPK, true>(m, (const T*)pot, (T)alpha, (const T*)in0,           \
-                                                         (const T*)in1, (T*)y0, (T*)y1, timeout_ns, st)        \
+                                                         (const T*)in1, (T*)y0, (T*)y1, pair_asm, timeout_ns, \
+                                                         st)                                                  \
                   : launch_apply_bulk_t<N, T, OPK, false>(m, (const T*)pot, (T)alpha, (const T*)in0,          \
-                                                          (const T*)in1, (T*)y0, (T*)y1, timeout_ns, st);
+                                                          (const T*)in1, (T*)y0, (T*)y1, pair_asm, timeout_ns, \
+                                                          st);
     if (!fp32) return cudaErrorInvalidValue;  // FP64 applies are FP64-pipe bound: one-pass kernel
     switch (op) {
         case OP_RES: SEM_BULK_CASE(float, OP_RES)
@@ -461,15 +463,17 @@ cudaError_t launch_update(const DevMesh& m, const double* p_in, const ZList& zl,
 }
 
 template <int N>
-cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, cudaStream_t st)
+cudaError_t launch_ring(const DevMesh& m, bool fp32, int mode, void* a0, void* a1, bool cross_only,
+                        cudaStream_t st)
 {
     const int tpb = 256;
-    const int grid = grid_for(m.n_pairs + m.n_bnd + m.n_nodes, tpb);
+    const long long np = cross_only ? m.n_pairs_x : m.n_pairs;
+    const int grid = grid_for(np + m.n_bnd + m.n_nodes, tpb);
 #define SEM_RING_CASE(T)                                                                                  \
     switch (mode) {                                                                                       \
-        case DSS_SUM: k_ring<N, T, DSS_SUM><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;             \
-        case DSS_MASK: k_ring<N, T, DSS_MASK><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;           \
-        default: k_ring<N, T, DSS_CONT><<<grid, tpb, 0, st>>>(m, (T*)a0, (T*)a1); break;                 \
+        case DSS_SUM: k_ring<N, T, DSS_SUM><<<grid, tpb, 0, st>>>(m, np, (T*)a0, (T*)a1); break;         \
+        case DSS_MASK: k_ring<N, T, DSS_MASK><<<grid, tpb, 0, st>>>(m, np, (T*)a0, (T*)a1); break;       \
+        default: k_ring<N, T, DSS_CONT><<<grid, tpb, 0, st>>>(m, np, (T*)a0, (T*)a1); break;             \
     }
     if (fp32) {
         SEM_RING_CASE(float)
@@ -506,9 +510,9 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
                                           cudaStream_t);                                             \
     template cudaError_t launch_dss<NV>(const DevMesh&, bool, int, double, const void*, void*,       \
                                         cudaStream_t);                                               \
-    template cudaError_t launch_ring<NV>(const DevMesh&, bool, int, void*, void*, cudaStream_t);     \
+    template cudaError_t launch_ring<NV>(const DevMesh&, bool, int, void*, void*, bool, cudaStream_t); \
     template cudaError_t launch_apply_bulk<NV>(const DevMesh&, int, bool, const void*, double,       \
-                                               const void*, const void*, void*, void*, bool,         \
+                                               const void*, const void*, void*, void*, bool, bool,   \
                                                long long, cudaStream_t);                             \
     template cudaError_t launch_unmask<NV>(const DevMesh&, bool, void*, cudaStream_t);               \
     template cudaError_t launch_mask<NV>(const DevMesh&, bool, void*, cudaStream_t);                 \

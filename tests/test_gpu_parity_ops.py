@@ -162,13 +162,22 @@ def test_in_place_ring_assembly_matches_separate_output(semlib, oracle, kind, p)
     assert rel_err(a.cpu().numpy(), om.apply_laplace(u)) <= TOL64
 
 
-@pytest.mark.parametrize("n,p", [(5, 1), (5, 8), (40, 4), (24, 8), (7, 13), (6, 16)])
-def test_pipelined_apply_matches_one_pass_kernel(semlib, oracle, n, p):
+@pytest.mark.parametrize("n,p,order", [(5, 1, "rows"), (5, 8, "rows"), (40, 4, "rows"), (24, 8, "rows"),
+                                         (7, 13, "rows"), (6, 16, "rows"), (24, 8, "shuffled"),
+                                         (9, 3, "shuffled")])
+def test_pipelined_apply_matches_one_pass_kernel(semlib, oracle, n, p, order):
     """the bulk-copy pipelined element kernel (mesh tails loaded with plain
-    loads) and the one-pass kernel give the same bits for every operator"""
+    loads; side pairs inside a batch summed by the kernel, the others by the
+    ring pass) and the one-pass kernel give the same bits for every operator,
+    in row order (most horizontal neighbours share a batch) and with the
+    elements shuffled and their corners rotated (few do)"""
     import torch
     from schrodingersem_gb300 import capi
     co, el = structured(n, box=(-1.0, 2.0, -0.5, 1.5), jitter=0.2, seed=n + p)
+    if order == "shuffled":
+        rng = np.random.default_rng(7 * n + p)
+        el = el[rng.permutation(len(el))]
+        el = np.stack([np.roll(row, int(r)) for row, r in zip(el, rng.integers(0, 4, len(el)))])
     ctx = semlib.Context(p, coords=co, elements=el)
     rng = np.random.default_rng(60 + p)
     shp = ctx.shape
