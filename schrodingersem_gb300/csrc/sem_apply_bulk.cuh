@@ -115,6 +115,14 @@ __host__ __device__ constexpr int bulk_tpb()
     return (sizeof(T) == 4 ? 128 : 64) * op_nc<OP>();
 }
 
+// threads of the kernel: with MG (Res) one thread per line works on both
+// components
+template <typename T, int OP, bool MG>
+__host__ __device__ constexpr int bulk_tpb_k()
+{
+    return MG ? bulk_tpb<T, OP>() / op_nc<OP>() : bulk_tpb<T, OP>();
+}
+
 constexpr int BULK_STAGES = 2;  // one batch in flight while one computes (3 measured slower)
 constexpr size_t BULK_SMEM_TARGET = 72 * 1024;  // three blocks per SM
 
@@ -148,7 +156,9 @@ struct DMat {
 
 // One batch = K elements.  After the stage of a batch has arrived (and, for
 // masked inputs, its non-owner ring copies are patched), thread
-// t = le*N + l works on line l of element le:
+// t = le*N + l works on line l of element le (with MG, Res only, on both
+// components, which shares the factor loads and fuses P3 with P4; without
+// MG, threads t and t + TPB/2 take the two components):
 //   P1  column l: ur(:,l) = D u(:,l) (kept in registers);
 //       row l:    us(l,:) = u(l,:) D^T          -> W1
 //   P2  column l: f1 = g11 ur - g12 us, f2 = g22 us - g12 ur; f2 -> W1,
@@ -158,8 +168,8 @@ struct DMat {
 // and W2 is written out with one bulk store per component.  Every
 // accumulation runs over k in ascending order as in apply_chunk (the
 // one-pass kernel), so both kernels give the same bits.
-template <int N, typename T, int OP, bool GATHER>
-__global__ void __launch_bounds__(bulk_tpb<T, OP>())
+template <int N, typename T, int OP, bool GATHER, bool MG>
+__global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
     k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
                  const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk, int pair_asm,
                  long long timeout_ns)
@@ -215,7 +225,7 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
     // (ring_src).  The table entries and values of a block's next batch are
     // loaded into registers while the current batch computes.
     constexpr int R = 4 * (N - 1);
-    constexpr int TPB = bulk_tpb<T, OP>();
+    constexpr int TPB = bulk_tpb_k<T, OP, MG>();
     constexpr int GQ = (K * R + TPB - 1) / TPB;
     int gsrc[GQ];
     T gval[GQ][NC];
@@ -316,6 +326,121 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
         }
         if (OP == OP_MASS) {
             for (int t = threadIdx.x; t < total; t += blockDim.x) y0[(long long)e0 * NN + t] = st[A_MASS * BN + t] * st[t];
+        } else if constexpr (MG) {
+            // Res, both components per thread: thread t works on line t
+            const int l0 = threadIdx.x;
+            const bool act = l0 < ne * N;
+            const int le = l0 / N, l = l0 - (l0 / N) * N;
+            const int base = le * NN;
+            T* w1a = W1 + base;
+            T* w1b = W1 + BN + base;
+            T* w2a = W2 + base;
+            T* w2b = W2 + BN + base;
+            if (threadIdx.x == 0 && store_bulk) bulk_wait_read();
+            __syncthreads();
+            T ura[N], urb[N];
+            // ---- P1: column l -> ur (registers); row l -> us (W1)
+            if (act) {
+                const T* ua = st + base;
+                const T* ub = st + BN + base;
+                T va[N], vb[N], aa[N], ab[N];
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    va[i] = ua[l * N + i];
+                    vb[i] = ub[l * N + i];
+                    ura[i] = T(0);
+                    urb[i] = T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int i = 0; i < N; ++i) {
+                        ura[i] = fma(D.d[i * N + k], va[k], ura[i]);
+                        urb[i] = fma(D.d[i * N + k], vb[k], urb[i]);
+                    }
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    va[j] = ua[j * N + l];
+                    vb[j] = ub[j * N + l];
+                    aa[j] = T(0);
+                    ab[j] = T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int j = 0; j < N; ++j) {
+                        aa[j] = fma(D.d[j * N + k], va[k], aa[j]);
+                        ab[j] = fma(D.d[j * N + k], vb[k], ab[j]);
+                    }
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    w1a[j * N + l] = aa[j];
+                    w1b[j * N + l] = ab[j];
+                }
+            }
+            __syncthreads();
+            // ---- P2: column l: fluxes (factors read once); f2 -> W1, lap1 = D^T f1 -> W2
+            if (act) {
+                T fa[N], fb[N], aa[N], ab[N];
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    const int q = base + l * N + i;
+                    const T g11 = st[A_G11 * BN + q], g12 = st[(A_G11 + 1) * BN + q], g22 = st[(A_G11 + 2) * BN + q];
+                    const T usa = w1a[l * N + i], usb = w1b[l * N + i];
+                    fa[i] = g11 * ura[i] - g12 * usa;
+                    fb[i] = g11 * urb[i] - g12 * usb;
+                    w1a[l * N + i] = g22 * usa - g12 * ura[i];
+                    w1b[l * N + i] = g22 * usb - g12 * urb[i];
+                    aa[i] = T(0);
+                    ab[i] = T(0);
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int i = 0; i < N; ++i) {
+                        aa[i] = fma(D.d[k * N + i], fa[k], aa[i]);
+                        ab[i] = fma(D.d[k * N + i], fb[k], ab[i]);
+                    }
+#pragma unroll
+                for (int i = 0; i < N; ++i) {
+                    w2a[l * N + i] = aa[i];
+                    w2b[l * N + i] = ab[i];
+                }
+            }
+            __syncthreads();
+            // ---- P3: row l: lap = lap1 + f2 D for both components, then the
+            // Res combination -> W1 (row l of W1 is read and written by this
+            // thread only)
+            if (act) {
+                T la[N], lb[N], fa[N], fb[N];
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    la[j] = w2a[j * N + l];
+                    lb[j] = w2b[j * N + l];
+                    fa[j] = w1a[j * N + l];
+                    fb[j] = w1b[j * N + l];
+                }
+#pragma unroll
+                for (int k = 0; k < N; ++k)
+#pragma unroll
+                    for (int j = 0; j < N; ++j) {
+                        la[j] = fma(D.d[k * N + j], fa[k], la[j]);
+                        lb[j] = fma(D.d[k * N + j], fb[k], lb[j]);
+                    }
+#pragma unroll
+                for (int j = 0; j < N; ++j) {
+                    const int q = base + j * N + l;
+                    const T ms = st[A_MASS * BN + q];
+                    const T pv = st[A_POT * BN + q];
+                    const T mv = ms * pv;
+                    const T u0 = st[q], u1 = st[BN + q];
+                    const T lap0 = la[j], lap1 = lb[j];
+                    const T Lv = lap1 + mv * u1;
+                    const T Lu = lap0 + mv * u0;
+                    W1[q] = ms * u0 + alpha * Lv;
+                    W1[BN + q] = alpha * Lu - ms * u1;
+                }
+            }
         } else {
             // thread t works on component c = t / LP, line t % LP
             constexpr int LP = TPB / NC;
@@ -426,6 +551,8 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
                     W1[c * BN + q] = o;
                 }
             }
+        }
+        if (OP != OP_MASS) {  // the staged result (W1): batch-internal side pairs, then the store
             if (pair_asm) {
                 __syncthreads();
 #pragma unroll
@@ -465,22 +592,23 @@ __global__ void __launch_bounds__(bulk_tpb<T, OP>())
 }
 
 // grid of k_apply_bulk for one instantiation (occupancy queried once per process)
-template <int N, typename T, int OP, bool GATHER>
-cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
-                                bool pair_asm, long long timeout_ns, cudaStream_t st)
+template <int N, typename T, int OP, bool GATHER, bool MG>
+cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
+                                 bool pair_asm, long long timeout_ns, cudaStream_t st)
 {
     static int blocks_per_sm = -1, sms = 0;
     constexpr size_t smem = bulk_smem_bytes<N, T, OP>();
+    constexpr int TPB = bulk_tpb_k<T, OP, MG>();
     if (blocks_per_sm < 0) {
-        cudaError_t e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER>,
+        cudaError_t e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER, MG>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         int dev = 0;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         int nb = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER>, bulk_tpb<T, OP>(),
-                                                                smem)) != cudaSuccess)
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER, MG>, TPB, smem)) !=
+            cudaSuccess)
             return e;
         blocks_per_sm = nb;
     }
@@ -495,9 +623,23 @@ cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T
     // batch-local pair tables exist for the FP32 Res batching only
     const int pa = (pair_asm && OP == OP_RES && sizeof(T) == 4 && m.bulk_K == K && m.bulk_pair_ptr) ? 1 : 0;
     if (pair_asm && !pa) return cudaErrorInvalidValue;
-    k_apply_bulk<N, T, OP, GATHER>
-        <<<grid, bulk_tpb<T, OP>(), smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
+    k_apply_bulk<N, T, OP, GATHER, MG>
+        <<<grid, TPB, smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
     return cudaGetLastError();
+}
+
+// Res with both components per thread, by degree: the FP32 sweep at about
+// 20 M nodes (L2 flushed) ran it 12-36 % faster for p = 2..11, 14 and 15 and
+// 3-10 % slower for p = 12, 13 and 16, where the batches hold only 4
+// elements and most of its threads have no line
+__host__ __device__ constexpr bool bulk_mg(int N) { return !(N == 13 || N == 14 || N == 17); }
+
+template <int N, typename T, int OP, bool GATHER>
+cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
+                                bool pair_asm, long long timeout_ns, cudaStream_t st)
+{
+    constexpr bool MG = OP == OP_RES && bulk_mg(N);
+    return launch_apply_bulk_mg<N, T, OP, GATHER, MG>(m, pot, alpha, in0, in1, y0, y1, pair_asm, timeout_ns, st);
 }
 
 }  // namespace semgb
