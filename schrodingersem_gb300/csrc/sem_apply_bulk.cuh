@@ -222,27 +222,30 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
     if (threadIdx.x == 0)
         for (int s = 0; s < S; ++s) issue(blockIdx.x + s * G, s);
     // masked input: ring copies that are not the owner take the owner's value
-    // (ring_src).  The table entries and values of a block's next batch are
-    // loaded into registers while the current batch computes.
+    // (ring_src).  The table entries of a block's batches are loaded two
+    // batches ahead and the owner values one batch ahead, so neither load
+    // is waited for while the batch that needs it is still to come.
     constexpr int R = 4 * (N - 1);
     constexpr int TPB = bulk_tpb_k<T, OP, MG>();
     constexpr int GQ = (K * R + TPB - 1) / TPB;
-    int gsrc[GQ];
-    T gval[GQ][NC];
-    auto gather_fetch = [&](long long bb) {
+    int gsrc[GQ], gsrc_n[GQ], gsrc_nn[GQ];  // tables of batches b, b+G, b+2G
+    T gval[GQ][NC], gval_n[GQ][NC];         // owner values of batches b, b+G
+    auto gather_tab = [&](long long bb, int (&dst)[GQ]) {
         const int neb = bb < nbatch ? min(K, m.E - (int)(bb * K)) : 0;
         const int nr = neb * R;
         const int* rs = m.ring_src + bb * K * R;
 #pragma unroll
         for (int q = 0; q < GQ; ++q) {
             const int t = threadIdx.x + q * TPB;
-            gsrc[q] = t < nr ? __ldg(rs + t) : -1;
+            dst[q] = t < nr ? __ldg(rs + t) : -1;
         }
+    };
+    auto gather_val = [&](const int (&src)[GQ], T (&dst)[GQ][NC]) {
 #pragma unroll
         for (int q = 0; q < GQ; ++q)
-            if (gsrc[q] >= 0) {
+            if (src[q] >= 0) {
 #pragma unroll
-                for (int c = 0; c < NC; ++c) gval[q][c] = arr[c][gsrc[q]];
+                for (int c = 0; c < NC; ++c) dst[q][c] = arr[c][src[q]];
             }
     };
     auto gather_apply = [&](T* st, int ne) {
@@ -271,25 +274,34 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
         }
     };
     // side pairs with both copies in the batch (pair_asm): owner += other,
-    // other = 0 in the staged result, before it is stored; the entries of the
-    // next batch are loaded while the current one computes
+    // other = 0 in the staged result, before it is stored.  Range of a batch's
+    // entries loaded two batches ahead, the entries one batch ahead.
     constexpr int PQ = (2 * K * (N - 2) + TPB - 1) / TPB > 0 ? (2 * K * (N - 2) + TPB - 1) / TPB : 1;
-    int ppair[PQ];
-    auto pair_fetch = [&](long long bb) {
-        int p0 = 0, p1 = 0;
+    int ppair[PQ], ppair_n[PQ];
+    int2 prng_n = make_int2(0, 0), prng_nn = make_int2(0, 0);  // entry ranges of batches b+G, b+2G
+    auto pair_rng = [&](long long bb) {
+        int2 r = make_int2(0, 0);
         if (pair_asm && bb < nbatch) {
-            p0 = __ldg(m.bulk_pair_ptr + bb);
-            p1 = __ldg(m.bulk_pair_ptr + bb + 1);
-            if (threadIdx.x == 0 && p1 - p0 > PQ * TPB) atomicExch(m.dev_err, 2);  // cannot happen: <= 2K(N-2)
+            r.x = __ldg(m.bulk_pair_ptr + bb);
+            r.y = __ldg(m.bulk_pair_ptr + bb + 1);
         }
+        return r;
+    };
+    auto pair_ent = [&](int2 r, int (&dst)[PQ]) {
+        if (threadIdx.x == 0 && r.y - r.x > PQ * TPB) atomicExch(m.dev_err, 2);  // cannot happen: <= 2K(N-2)
 #pragma unroll
         for (int q = 0; q < PQ; ++q) {
-            const int t = p0 + threadIdx.x + q * TPB;
-            ppair[q] = t < p1 ? __ldg(m.bulk_pairs + t) : -1;
+            const int t = r.x + threadIdx.x + q * TPB;
+            dst[q] = t < r.y ? __ldg(m.bulk_pairs + t) : -1;
         }
     };
-    if (GATHER) gather_fetch(blockIdx.x);
-    pair_fetch(blockIdx.x);
+    if (GATHER) {
+        gather_tab(blockIdx.x, gsrc);
+        gather_val(gsrc, gval);
+        gather_tab(blockIdx.x + G, gsrc_n);
+    }
+    pair_ent(pair_rng(blockIdx.x), ppair);
+    prng_n = pair_rng(blockIdx.x + G);
     int it = 0;
     for (long long b = blockIdx.x; b < nbatch; b += G, ++it) {
         const int s = it % S;
@@ -322,7 +334,12 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
         if (GATHER) {
             gather_apply(st, ne);
             __syncthreads();
-            gather_fetch(b + G);  // in flight while this batch computes
+            gather_val(gsrc_n, gval_n);  // in flight while this batch computes
+            gather_tab(b + 2 * G, gsrc_nn);
+        }
+        if (pair_asm) {
+            pair_ent(prng_n, ppair_n);
+            prng_nn = pair_rng(b + 2 * G);
         }
         if (OP == OP_MASS) {
             for (int t = threadIdx.x; t < total; t += blockDim.x) y0[(long long)e0 * NN + t] = st[A_MASS * BN + t] * st[t];
@@ -565,7 +582,6 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                         W1[cc * BN + px] = T(0);
                     }
                 }
-                pair_fetch(b + G);
             }
             fence_proxy_async_smem();
             __syncthreads();
@@ -581,6 +597,21 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
 #pragma unroll
                     for (int cc = 0; cc < NC; ++cc) outp[cc][(long long)e0 * NN + t] = W1[cc * BN + t];
             }
+        }
+        // the next batch's tables and values (loaded during this one)
+        if (GATHER) {
+#pragma unroll
+            for (int q = 0; q < GQ; ++q) {
+                gsrc[q] = gsrc_n[q];
+                gsrc_n[q] = gsrc_nn[q];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) gval[q][c] = gval_n[q][c];
+            }
+        }
+        if (pair_asm) {
+#pragma unroll
+            for (int q = 0; q < PQ; ++q) ppair[q] = ppair_n[q];
+            prng_n = prng_nn;
         }
         // stage s free; this thread's shared-memory accesses ordered before
         // the bulk copy that refills it
