@@ -482,6 +482,15 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
     // corner copies in CSR order per element corner (the gathers read them
     // with one dependent load instead of three)
     std::vector<int> corner_nb((size_t)n_el * 4 * CORNER_NB_MAX, -1), corner_cnt4(n_el, 0);
+    std::vector<int> node_nb((size_t)n_nodes * CORNER_NB_MAX, -1);
+    for (int node = 0; node < n_nodes; ++node) {
+        const int q0 = nptr[node], cnt = nptr[node + 1] - q0;
+        int* dst = &node_nb[(size_t)node * CORNER_NB_MAX];
+        if (cnt > CORNER_NB_MAX)
+            dst[0] = -2;
+        else
+            for (int q = 0; q < cnt; ++q) dst[q] = nflat[q0 + q];
+    }
     for (int e = 0; e < n_el; ++e)
         for (int cc = 0; cc < 4; ++cc) {
             const int node = cnode[4 * e + cc];
@@ -695,6 +704,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, fL, &d.fdmL64)) || (s = upload(c, tof(fL), &d.fdmL32)) || (s = upload(c, fel, &d.fdm_el)) ||
         (s = upload(c, ring_src, &d.ring_src)) || (s = upload(c, edge_pairs, &d.edge_pairs)) ||
         (s = upload(c, corner_nb, &d.corner_nb)) || (s = upload(c, corner_cnt4, &d.corner_cnt4)) ||
+        (s = upload(c, node_nb, &d.node_nb)) ||
         (s = upload(c, bulk_pair_ptr, &d.bulk_pair_ptr)) ||
         (!bulk_pairs.empty() && (s = upload(c, bulk_pairs, &d.bulk_pairs))) ||
         (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)))

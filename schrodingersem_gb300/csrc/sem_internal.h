@@ -10,7 +10,8 @@ namespace semgb {
 
 constexpr int MIN_N = 2;   // p = 1
 constexpr int MAX_N = 17;  // p = 16
-constexpr int CORNER_NB_MAX = 8;  // copies per corner node held in DevMesh::corner_nb
+constexpr int CORNER_NB_MAX = 8;  // copies per corner node held in DevMesh::corner_nb / node_nb
+static_assert(CORNER_NB_MAX % 4 == 0, "node_nb rows are read as int4");
 
 // Element-local operator kinds (the closures of the reference's drivers).
 enum OpKind : int {
@@ -75,6 +76,8 @@ struct DevMesh {
     // corner_cnt4[e] packs the four corners' copy counts, 8 bits each
     const int* corner_nb = nullptr;
     const int* corner_cnt4 = nullptr;
+    // the same lists per corner node (n_nodes rows of CORNER_NB_MAX)
+    const int* node_nb = nullptr;
     const int2* edge_pairs = nullptr;
     const int* bnd_flat = nullptr;
     const char* node_bnd = nullptr;

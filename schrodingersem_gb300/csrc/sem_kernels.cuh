@@ -102,23 +102,60 @@ __global__ void k_ring(DevMesh m, long long np, T* __restrict__ a0, T* __restric
             for (int q = 0; q < 2; ++q)
                 if (planes[q]) planes[q][f] = T(0);
         } else {
+            // corner node: its copies in CSR order from one padded row (two
+            // dependent loads: the row, the values), else the CSR
             const int node = (int)(it - np - nb);
-            const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
-            if (q1 <= q0) continue;
+            const int4* row = reinterpret_cast<const int4*>(m.node_nb + (size_t)node * CORNER_NB_MAX);
+            int f[CORNER_NB_MAX];
+#pragma unroll
+            for (int h = 0; h < CORNER_NB_MAX / 4; ++h) {
+                const int4 v = __ldg(row + h);
+                f[4 * h] = v.x;
+                f[4 * h + 1] = v.y;
+                f[4 * h + 2] = v.z;
+                f[4 * h + 3] = v.w;
+            }
             const bool bnd = __ldg(m.node_bnd + node) != 0;
+            if (f[0] == -2) {
+                const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
+#pragma unroll
+                for (int q = 0; q < 2; ++q) {
+                    T* a = planes[q];
+                    if (!a) continue;
+                    if (bnd) {
+                        if (MODE != DSS_SUM)
+                            for (int t = q0; t < q1; ++t) a[__ldg(m.node_flat + t)] = T(0);
+                        continue;
+                    }
+                    T sum = T(0);
+                    for (int t = q0; t < q1; ++t) sum += a[__ldg(m.node_flat + t)];
+                    for (int t = q0; t < q1; ++t)
+                        a[__ldg(m.node_flat + t)] = (MODE == DSS_MASK && t != q0) ? T(0) : sum;
+                }
+                continue;
+            }
+            if (f[0] < 0) continue;  // no copies
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
                 T* a = planes[q];
                 if (!a) continue;
                 if (bnd) {
                     if (MODE != DSS_SUM)
-                        for (int t = q0; t < q1; ++t) a[__ldg(m.node_flat + t)] = T(0);
+#pragma unroll
+                        for (int k = 0; k < CORNER_NB_MAX; ++k)
+                            if (f[k] >= 0) a[f[k]] = T(0);
                     continue;
                 }
+                T v[CORNER_NB_MAX];
+#pragma unroll
+                for (int k = 0; k < CORNER_NB_MAX; ++k) v[k] = f[k] >= 0 ? a[f[k]] : T(0);
                 T sum = T(0);
-                for (int t = q0; t < q1; ++t) sum += a[__ldg(m.node_flat + t)];
-                for (int t = q0; t < q1; ++t)
-                    a[__ldg(m.node_flat + t)] = (MODE == DSS_MASK && t != q0) ? T(0) : sum;
+#pragma unroll
+                for (int k = 0; k < CORNER_NB_MAX; ++k)
+                    if (f[k] >= 0) sum += v[k];
+#pragma unroll
+                for (int k = 0; k < CORNER_NB_MAX; ++k)
+                    if (f[k] >= 0) a[f[k]] = (MODE == DSS_MASK && k != 0) ? T(0) : sum;
             }
         }
     }
