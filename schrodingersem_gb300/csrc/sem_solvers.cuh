@@ -206,6 +206,57 @@ __device__ __forceinline__ void scal_step_rsqrt(MinresScal<T>& sc, double alpha_
     sc.tpinvb = (T)sc.pinvb;
 }
 
+// One node of MINRES Phase B: Av = DSS(Y)/beta, y = Av - c1 r1, the
+// alpha partial v.y, and (pending) the w / x update of the previous
+// iteration.  The vectors arrive as restrict pointers (distinct buffers), so
+// that once inlined into an unrolled node loop the loads of the next node
+// can be issued before the stores of this one.
+template <int N, typename T, int NC, int PRE>
+__device__ __forceinline__ void phase_b_node(const DevMesh& m, long long n, long long idx, int it, bool pending,
+                                             T inv_b, T c1, T tpg, T tpeps, T tpdelta, T tpphi, T tpinvb,
+                                             const T* __restrict__ Ycur, const T* __restrict__ Lr1,
+                                             const T* __restrict__ Zc, const T* __restrict__ Zq,
+                                             const T* __restrict__ W1, const T* __restrict__ W2,
+                                             const T* __restrict__ pinv, T* __restrict__ Ly, T* __restrict__ Wn,
+                                             T* __restrict__ x0, T* __restrict__ x1, T& s1)
+{
+    constexpr int NN = N * N;
+    const int e = (int)(idx / NN);
+    const int node = (int)(idx - (long long)e * NN);
+    const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+    const bool own = ni_owner(ni);
+    const T pv = PRE == 1 ? pinv[idx] : T(1);
+    T av[NC], r1v[NC], zc[NC], zp[NC], w1v[NC], w2v[NC], xv[NC];
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const long long q = c * n + idx;
+        av[c] = dss_value<N, T, DSS_CONT>(m, Ycur + c * n, ni, e, idx);
+        r1v[c] = it >= 2 ? Lr1[q] : T(0);
+        zc[c] = Zc[q];
+        if (pending) {
+            zp[c] = PRE == 2 ? Zq[q] : T(0);
+            w1v[c] = W1[q];
+            w2v[c] = W2[q];
+            if (own) xv[c] = (c == 0 ? x0 : x1)[idx];
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+        const long long q = c * n + idx;
+        const T a = av[c] * inv_b;
+        const T y3 = it >= 2 ? a - c1 * r1v[c] : a;
+        const T vv = inv_b * (PRE == 1 ? pv * zc[c] : zc[c]);
+        if (own) s1 = fma(vv, y3, s1);
+        Ly[q] = y3;
+        if (pending) {
+            const T vprev = tpinvb * (PRE == 2 ? zp[c] : PRE == 1 ? pv * r1v[c] : r1v[c]);
+            const T wn = tpg * ((vprev - tpeps * w1v[c]) - tpdelta * w2v[c]);
+            Wn[q] = wn;
+            if (own) (c == 0 ? x0 : x1)[idx] = xv[c] + tpphi * wn;
+        }
+    }
+}
+
 // include/minres.hpp:19-107 inside a cooperative kernel.  Lanczos vectors
 // are kept in the continuous format (every copy of a shared node holds the
 // assembled value, boundary zero) so the operator needs no gather; dots
@@ -335,62 +386,14 @@ __device__ __forceinline__ bool minres_core(T* sm, int kmax, double* red, Minres
             const T tpg = sc.tpg, tpeps = sc.tpeps, tpdelta = sc.tpdelta, tpphi = sc.tpphi, tpinvb = sc.tpinvb;
             const T* Ycur = w.Y[(it - 1) & 1];
             T s1 = T(0);
-            // two nodes per thread and pass: every load of both is issued
-            // before the first store (the stores may alias the loaded
-            // vectors as far as the compiler knows)
-            constexpr int U = 1;
             const T* Zc = PRE == 2 ? w.Z[(it - 1) & 1] : L[ir2];
             const T* Zq = PRE == 2 ? w.Z[it & 1] : nullptr;
-            for (long long i0 = nb + threadIdx.x; i0 < ne; i0 += U * (long long)blockDim.x) {
-                long long ix[U];
-                bool val[U], own[U];
-                T av[U][NC], r1v[U][NC], zc[U][NC], zp[U][NC], w1v[U][NC], w2v[U][NC], pv[U];
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    ix[u] = i0 + u * (long long)blockDim.x;
-                    val[u] = ix[u] < ne;
-                    own[u] = false;
-                    if (!val[u]) continue;
-                    const long long idx = ix[u];
-                    const int e = (int)(idx / NN);
-                    const int node = (int)(idx - (long long)e * NN);
-                    const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
-                    own[u] = ni_owner(ni);
-                    pv[u] = PRE == 1 ? pinv[idx] : T(1);
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        const long long q = c * n + idx;
-                        av[u][c] = dss_value<N, T, DSS_CONT>(m, Ycur + c * n, ni, e, idx);
-                        r1v[u][c] = it >= 2 ? L[ir1][q] : T(0);
-                        zc[u][c] = Zc[q];
-                        if (pending) {
-                            zp[u][c] = PRE == 2 ? Zq[q] : T(0);
-                            w1v[u][c] = W[iw1][q];
-                            w2v[u][c] = W[iw2][q];
-                        }
-                    }
-                }
-#pragma unroll
-                for (int u = 0; u < U; ++u) {
-                    if (!val[u]) continue;
-                    const long long idx = ix[u];
-#pragma unroll
-                    for (int c = 0; c < NC; ++c) {
-                        const long long q = c * n + idx;
-                        const T a = av[u][c] * inv_b;
-                        const T y3 = it >= 2 ? a - c1 * r1v[u][c] : a;
-                        const T vv = inv_b * (PRE == 1 ? pv[u] * zc[u][c] : zc[u][c]);
-                        if (own[u]) s1 = fma(vv, y3, s1);
-                        L[iy][q] = y3;
-                        if (pending) {
-                            const T vprev = tpinvb * (PRE == 2 ? zp[u][c] : PRE == 1 ? pv[u] * r1v[u][c] : r1v[u][c]);
-                            const T wn = tpg * ((vprev - tpeps * w1v[u][c]) - tpdelta * w2v[u][c]);
-                            W[iw][q] = wn;
-                            if (own[u]) xp[c][idx] += tpphi * wn;
-                        }
-                    }
-                }
-            }
+            T* const x1 = NC == 2 ? xp[1] : nullptr;
+#pragma unroll 2
+            for (long long idx = nb + threadIdx.x; idx < ne; idx += blockDim.x)
+                phase_b_node<N, T, NC, PRE>(m, n, idx, it, pending, inv_b, c1, tpg, tpeps, tpdelta, tpphi, tpinvb,
+                                            Ycur, L[ir1], Zc, Zq, W[iw1], W[iw2], pinv, L[iy], W[iw], xp[0], x1,
+                                            s1);
             if (pending) {
                 const int tmp = iw1;
                 iw1 = iw2;
