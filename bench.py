@@ -170,7 +170,7 @@ def run_reference(args):
             "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "form": "reference OpenMP path (CPU oracle port)"},
             "cpu_baseline": {"value": sps, "unit": "s/step", "cores": threads, "kind": "port",
-                             "sample": f"{len(timed)} timed SDIRK4-3 steps after {args.warmup} warm-up, "
+                             "sample": f"{len(timed)} timed SDIRK4-3 steps after {warm} warm-up, "
                                        f"OpenMP {threads} threads"},
             "e2e": {"value": sps, "unit": "s/step", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
