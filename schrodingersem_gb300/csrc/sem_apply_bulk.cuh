@@ -17,6 +17,7 @@
 // in flight and returns.
 #pragma once
 #include <cstdint>
+#include <cstring>
 
 #include "sem_device.cuh"
 
@@ -154,6 +155,63 @@ struct DMat {
     T d[N * N];
 };
 
+// D(i,k) duplicated into both lanes of a packed FP32 pair, for the paired
+// FMA of the two Res components (each lane an IEEE FP32 FMA: same bits as
+// two scalar FMAs)
+template <int N>
+struct DMat2 {
+    unsigned long long d[N * N];
+};
+__device__ __forceinline__ unsigned long long f2pack(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void f2unpack(unsigned long long v, float& a, float& b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ unsigned long long f2fma(unsigned long long a, unsigned long long b, unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Line contraction of both Res components: oa[o] = ca[o] + sum_k M(o,k) a[k]
+// (and b) with M = D (TR false) or D^T (TR true), k ascending; paired FP32
+// FMAs when F2 (measured faster for N <= 11, slower above), else scalar.
+template <int N, bool TR, bool F2>
+__device__ __forceinline__ void contract2(const DMat<N, float>& D, const DMat2<N>& D2, const float* a,
+                                          const float* b, float* oa, float* ob)
+{
+    if constexpr (F2) {
+        unsigned long long v[N], acc[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+            v[i] = f2pack(a[i], b[i]);
+            acc[i] = f2pack(oa[i], ob[i]);
+        }
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+#pragma unroll
+            for (int o = 0; o < N; ++o) acc[o] = f2fma(D2.d[TR ? k * N + o : o * N + k], v[k], acc[o]);
+#pragma unroll
+        for (int o = 0; o < N; ++o) f2unpack(acc[o], oa[o], ob[o]);
+    } else {
+#pragma unroll
+        for (int k = 0; k < N; ++k)
+#pragma unroll
+            for (int o = 0; o < N; ++o) {
+                const float dk = D.d[TR ? k * N + o : o * N + k];
+                oa[o] = fma(dk, a[k], oa[o]);
+                ob[o] = fma(dk, b[k], ob[o]);
+            }
+    }
+}
+__host__ __device__ constexpr bool bulk_f2(int N) { return N <= 11; }
+
 // One batch = K elements.  After the stage of a batch has arrived (and, for
 // masked inputs, its non-owner ring copies are patched), thread
 // t = le*N + l works on line l of element le (with MG, Res only, on both
@@ -170,7 +228,7 @@ struct DMat {
 // one-pass kernel), so both kernels give the same bits.
 template <int N, typename T, int OP, bool GATHER, bool MG>
 __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
-    k_apply_bulk(DevMesh m, DMat<N, T> D, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
+    k_apply_bulk(DevMesh m, DMat<N, T> D, DMat2<N> D2, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
                  const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk, int pair_asm,
                  long long timeout_ns)
 {
@@ -368,13 +426,7 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                     ura[i] = T(0);
                     urb[i] = T(0);
                 }
-#pragma unroll
-                for (int k = 0; k < N; ++k)
-#pragma unroll
-                    for (int i = 0; i < N; ++i) {
-                        ura[i] = fma(D.d[i * N + k], va[k], ura[i]);
-                        urb[i] = fma(D.d[i * N + k], vb[k], urb[i]);
-                    }
+                contract2<N, false, bulk_f2(N)>(D, D2, va, vb, ura, urb);
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     va[j] = ua[j * N + l];
@@ -382,13 +434,7 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                     aa[j] = T(0);
                     ab[j] = T(0);
                 }
-#pragma unroll
-                for (int k = 0; k < N; ++k)
-#pragma unroll
-                    for (int j = 0; j < N; ++j) {
-                        aa[j] = fma(D.d[j * N + k], va[k], aa[j]);
-                        ab[j] = fma(D.d[j * N + k], vb[k], ab[j]);
-                    }
+                contract2<N, false, bulk_f2(N)>(D, D2, va, vb, aa, ab);
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     w1a[j * N + l] = aa[j];
@@ -411,13 +457,7 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                     aa[i] = T(0);
                     ab[i] = T(0);
                 }
-#pragma unroll
-                for (int k = 0; k < N; ++k)
-#pragma unroll
-                    for (int i = 0; i < N; ++i) {
-                        aa[i] = fma(D.d[k * N + i], fa[k], aa[i]);
-                        ab[i] = fma(D.d[k * N + i], fb[k], ab[i]);
-                    }
+                contract2<N, true, bulk_f2(N)>(D, D2, fa, fb, aa, ab);
 #pragma unroll
                 for (int i = 0; i < N; ++i) {
                     w2a[l * N + i] = aa[i];
@@ -437,13 +477,7 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                     fa[j] = w1a[j * N + l];
                     fb[j] = w1b[j * N + l];
                 }
-#pragma unroll
-                for (int k = 0; k < N; ++k)
-#pragma unroll
-                    for (int j = 0; j < N; ++j) {
-                        la[j] = fma(D.d[k * N + j], fa[k], la[j]);
-                        lb[j] = fma(D.d[k * N + j], fb[k], lb[j]);
-                    }
+                contract2<N, true, bulk_f2(N)>(D, D2, fa, fb, la, lb);
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     const int q = base + j * N + l;
@@ -646,7 +680,16 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
     if (!m.Dh) return cudaErrorInvalidValue;
     DMat<N, T> D;
-    for (int i = 0; i < N * N; ++i) D.d[i] = (T)m.Dh[i];
+    DMat2<N> D2 = {};
+    for (int i = 0; i < N * N; ++i) {
+        D.d[i] = (T)m.Dh[i];
+        if (MG) {
+            const float f = (float)m.Dh[i];
+            uint32_t u;
+            memcpy(&u, &f, sizeof(u));
+            D2.d[i] = ((unsigned long long)u << 32) | u;
+        }
+    }
     constexpr int K = bulk_k<T, OP>(N);
     const long long nbatch = (m.E + K - 1) / K;
     const int grid = (int)std::min<long long>(nbatch, (long long)sms * blocks_per_sm);
@@ -655,7 +698,7 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     const int pa = (pair_asm && OP == OP_RES && sizeof(T) == 4 && m.bulk_K == K && m.bulk_pair_ptr) ? 1 : 0;
     if (pair_asm && !pa) return cudaErrorInvalidValue;
     k_apply_bulk<N, T, OP, GATHER, MG>
-        <<<grid, TPB, smem, st>>>(m, D, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
+        <<<grid, TPB, smem, st>>>(m, D, D2, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
     return cudaGetLastError();
 }
 
