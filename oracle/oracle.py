@@ -50,9 +50,7 @@ _CB = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_int, _dp, _dp, _ip, C.c_int)
 
 def build(force: bool = False) -> str:
     """Compile the oracle with its Makefile (gcc, OpenMP)."""
-    src = os.path.join(_HERE, "sem_oracle.c")
-    if force or not os.path.exists(_LIB_PATH) or os.path.getmtime(_LIB_PATH) < os.path.getmtime(src):
-        subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    subprocess.run(["make", "-s", "-C", _HERE] + (["-B"] if force else []), check=True)
     return _LIB_PATH
 
 

@@ -208,6 +208,48 @@ static long pair_key(int a, int b, int n_nodes)
     return (long)lo * (long)n_nodes + hi;
 }
 
+/* Cantor's pairing of the sorted corner pair, in the reference's int
+ * arithmetic (load_mesh.hpp:17-22, 146-149); the product is formed in 32-bit
+ * two's complement so meshes whose sums pass 65535 key as the reference's
+ * wrapped ints do. */
+static int cantor_key(int a, int b)
+{
+    int x = a < b ? a : b, y = a < b ? b : a;
+    unsigned s = (unsigned)x + (unsigned)y;
+    int prod = (int)(s * (s + 1u));
+    return (int)((unsigned)(prod / 2) + (unsigned)y);
+}
+
+void or_stl_edge_order(int n_edges, const int* keys, int* order);
+
+/* Mesh::edges follows the iteration order of load_mesh's unordered_map
+ * (load_mesh.hpp:181-206); see edge_order.cpp. */
+static void reorder_edges_like_reference(or_mesh* m)
+{
+    static const int emap1[] = {0, 1, 3, 0}, emap2[] = {1, 2, 2, 3};
+    const int ne = m->n_edges;
+    int* keys = (int*)malloc(sizeof(int) * (ne > 0 ? ne : 1));
+    int* order = (int*)malloc(sizeof(int) * (ne > 0 ? ne : 1));
+    for (int ed = 0; ed < ne; ++ed) {
+        int e = m->edge_el[2 * ed], s = m->edge_side[2 * ed];
+        keys[ed] = cantor_key(m->corner_ids[4 * e + emap1[s - 1]], m->corner_ids[4 * e + emap2[s - 1]]);
+    }
+    or_stl_edge_order(ne, keys, order);
+    int* t = (int*)malloc(sizeof(int) * 2 * (ne > 0 ? ne : 1));
+#define PERMUTE1(arr) do { for (int k = 0; k < ne; ++k) t[k] = arr[order[k]]; memcpy(arr, t, sizeof(int) * ne); } while (0)
+#define PERMUTE2(arr) do { for (int k = 0; k < ne; ++k) { t[2 * k] = arr[2 * order[k]]; t[2 * k + 1] = arr[2 * order[k] + 1]; } memcpy(arr, t, sizeof(int) * 2 * ne); } while (0)
+    PERMUTE1(m->edge_type);
+    PERMUTE1(m->edge_start);
+    PERMUTE1(m->edge_delta);
+    PERMUTE2(m->edge_el);
+    PERMUTE2(m->edge_side);
+#undef PERMUTE1
+#undef PERMUTE2
+    free(t);
+    free(keys);
+    free(order);
+}
+
 or_mesh* or_mesh_create(int p, int n_nodes, const double* coords, int n_el, const int* elements)
 {
     if (p < 1 || n_nodes <= 0 || n_el <= 0) return NULL;
@@ -307,6 +349,7 @@ or_mesh* or_mesh_create(int p, int n_nodes, const double* coords, int n_el, cons
         }
     free(tab);
     m->n_edges = ne;
+    reorder_edges_like_reference(m);
     /* boundary flags and orientation (load_mesh.hpp:181-206) */
     for (int ed = 0; ed < ne; ++ed) {
         if (m->edge_type[ed] == OR_BOUNDARY) {
