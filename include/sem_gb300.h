@@ -53,6 +53,11 @@ enum sem_status {
 #define SEM_FLAG_METRIC_CORRECTED 0x1u /* C(i,j) = (Y_xi[j]^2 + X_xi[j]^2)/J.  Without this
                                           flag the reference's formula include/Quad.hpp:53
                                           (Y_xi[i]^2) is reproduced, for parity. */
+#define SEM_FLAG_NEUMANN 0x2u /* natural (Neumann) boundary: boundary edges and corners
+                                 stay degrees of freedom, owned by their first element and
+                                 never masked (the reference zeroes them for Dirichlet data,
+                                 include/mask_side.hpp:28-30, mask_node.hpp:13-21).  Every
+                                 operator, solver and driver of the context follows it. */
 
 /* options for sem_ctx_set_option */
 enum sem_option {
@@ -224,8 +229,10 @@ int sem_apply_schro_res_f32(sem_ctx* ctx, const float* V, float alpha,
  * the call allocates nothing.  Requires 2*E*N*N <= 1048576, otherwise it
  * returns SEM_ERR_UNSUPPORTED.  The first call on each device looks up the
  * array's device address; make that first call before any stream capture.
- * All calls share the array: calls whose kernels overlap on the GPU (other
- * streams, other contexts) race on it.  Device pointers. */
+ * The context's device must be current (else SEM_ERR_ARG).  Outputs may
+ * alias the inputs (in place).  All calls share the array: calls whose
+ * kernels overlap on the GPU (other streams, other contexts) race on it.
+ * Device pointers. */
 int sem_apply_schro_res_noalloc(sem_ctx* ctx, const double* V, double alpha,
                                 const double* q_re, const double* q_im,
                                 double* out_re, double* out_im);
@@ -254,6 +261,29 @@ int sem_poisson(sem_ctx* ctx, double* u, const double* f, int max_iter, double t
 /* schro_omp::helmholtz (include/openmp_impl/helmholtz.hpp:18-64) */
 int sem_helmholtz(sem_ctx* ctx, double* u, const double* c, const double* f,
                   int max_iter, double tol, sem_solver_results* res);
+/* Poisson and Helmholtz with boundary data, no counterpart in the reference
+ * (whose masks zero every boundary copy: include/mask_side.hpp:28-30).
+ *  - Dirichlet context (default): u = g on the boundary.  g is an
+ *    element-local field (E*N*N) of which the copies of boundary nodes are
+ *    read.  By lifting: with u_D = g on those copies and 0 elsewhere, the
+ *    masked system A u0 = gproj(f) - A u_D is solved (PCG / MINRES as
+ *    sem_poisson / sem_helmholtz) and u = u0 + u_D.
+ *  - SEM_FLAG_NEUMANN context: du/dn = g on the boundary.  g holds the
+ *    outward normal derivative per element side node, E*4*N values: side s
+ *    (0: j = 0, 1: i = N-1, 2: j = N-1, 3: i = 0), node k = 0..N-1 along the
+ *    side (the element's i on sides 0 and 2, its j on sides 1 and 3); only
+ *    boundary sides are read (a domain corner takes each side's own value).
+ *    The boundary integral of the weak form, sum over boundary sides of
+ *    w_k (L/2) g_k (GLL quadrature on the straight side of length L), is
+ *    added to gproj(f).  Poisson with only Neumann data is singular; use
+ *    Helmholtz with c > 0 there.
+ * u in: initial guess (its boundary copies are ignored for Dirichlet data);
+ * out: the solution at every copy (continuous format).  Host or device
+ * pointers. */
+int sem_poisson_bc(sem_ctx* ctx, double* u, const double* f, const double* g, int max_iter,
+                   double tol, sem_solver_results* res);
+int sem_helmholtz_bc(sem_ctx* ctx, double* u, const double* c, const double* f, const double* g,
+                     int max_iter, double tol, sem_solver_results* res);
 /* schro_omp::schrodinger_bdf2 (include/openmp_impl/schrodinger.hpp:22-128) */
 int sem_schrodinger_bdf2(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
                          double T, const sem_solver_opts* opts,

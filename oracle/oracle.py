@@ -68,6 +68,7 @@ def lib():
         L.or_mesh_load.argtypes = [C.c_int, C.c_char_p]
         L.or_mesh_load.restype = C.POINTER(_OrMesh)
         L.or_mesh_compute_metrics.argtypes = [C.POINTER(_OrMesh), C.c_int]
+        L.or_mesh_set_neumann.argtypes = [C.POINTER(_OrMesh)]
         L.or_mesh_free.argtypes = [C.POINTER(_OrMesh)]
         L.or_mesh_dof.argtypes = [C.POINTER(_OrMesh)]
         L.or_mesh_node_coords.argtypes = [C.POINTER(_OrMesh), _dp, _dp]
@@ -164,7 +165,8 @@ def legendre_p(n: int, x: float) -> float:
 class Mesh:
     """The oracle's mesh: topology (load_mesh.hpp) + metrics (Quad.hpp)."""
 
-    def __init__(self, p: int, coords=None, elements=None, folder: str | None = None, ref_compat: bool = True):
+    def __init__(self, p: int, coords=None, elements=None, folder: str | None = None, ref_compat: bool = True,
+                 neumann: bool = False):
         L = lib()
         if folder is not None:
             ptr = L.or_mesh_load(int(p), folder.encode())
@@ -177,6 +179,9 @@ class Mesh:
             raise ValueError("oracle: could not build mesh")
         self._ptr = ptr
         L.or_mesh_compute_metrics(ptr, 1 if ref_compat else 0)
+        self.neumann = bool(neumann)
+        if neumann:
+            L.or_mesh_set_neumann(ptr)
         m = ptr.contents
         self.p, self.N, self.n_nodes, self.n_el, self.n_edges = m.p, m.N, m.n_nodes, m.n_el, m.n_edges
         N, E = self.N, self.n_el
@@ -190,6 +195,10 @@ class Mesh:
         self.node_ptr = np.ctypeslib.as_array(m.node_ptr, (self.n_nodes + 1,)).copy()
         self.node_el = np.ctypeslib.as_array(m.node_el, (4 * E,)).copy()
         self.corner_ids = np.ctypeslib.as_array(m.corner_ids, (4 * E,)).reshape(E, 4).copy()
+        self.xs = np.ctypeslib.as_array(m.xs, (4 * E,)).reshape(E, 4).copy()
+        self.ys = np.ctypeslib.as_array(m.ys, (4 * E,)).reshape(E, 4).copy()
+        self.node_i = np.ctypeslib.as_array(m.node_i, (4 * E,)).copy()
+        self.node_j = np.ctypeslib.as_array(m.node_j, (4 * E,)).copy()
         sh = (E, N, N)
         self.J = np.ctypeslib.as_array(m.J, (E * N * N,)).reshape(sh).copy()
         self.A = np.ctypeslib.as_array(m.A, (E * N * N,)).reshape(sh).copy()
@@ -312,3 +321,69 @@ class Mesh:
         cb = _CB(_cb)
         ok = fn(self._ptr, _p(pr), _p(pi), _p(V), float(T), C.byref(opts), cb, None)
         return pr, pi, bool(ok)
+
+    # ---- boundary data (no counterpart in the reference) ----
+    def _side_index(self, s0: int):
+        """(j, i) index arrays of the N nodes of library side s0 (0: j = 0,
+        1: i = N-1, 2: j = N-1, 3: i = 0), k along the element's own i (sides
+        0, 2) or j (sides 1, 3)"""
+        N = self.N
+        k = np.arange(N)
+        return {0: (np.zeros(N, int), k), 1: (k, np.full(N, N - 1)), 2: (np.full(N, N - 1), k),
+                3: (k, np.zeros(N, int))}[s0]
+
+    def bc_field(self, g):
+        """Dirichlet mesh: the lifting u_D (g at every copy of a boundary node,
+        0 elsewhere), g element-local.  Neumann mesh: the boundary integral
+        w_k (L/2) g[e, s, k] at node k of every boundary side s of length L,
+        g of shape (E, 4, N) (outward normal derivative per side node)."""
+        F = self.zeros()
+        g = np.asarray(g, dtype=np.float64)
+        ca, cb = (0, 1, 3, 0), (1, 2, 2, 3)
+        for ed in range(self.n_edges):
+            if self.edge_type[ed] != 1:
+                continue
+            e, s0 = int(self.edge_el[ed, 0]), int(self.edge_side[ed, 0]) - 1
+            jj, ii = self._side_index(s0)
+            if self.neumann:
+                L = np.hypot(self.xs[e, cb[s0]] - self.xs[e, ca[s0]], self.ys[e, cb[s0]] - self.ys[e, ca[s0]])
+                F[e, jj, ii] += self.w * (0.5 * L) * g[e, s0, :]
+            else:
+                F[e, jj, ii] = g[e, jj, ii]
+        if not self.neumann:
+            for c in range(self.n_nodes):
+                if self.node_type[c] != 1:
+                    continue
+                for q in range(self.node_ptr[c], self.node_ptr[c + 1]):
+                    e, i, j = self.node_el[q], self.node_i[q], self.node_j[q]
+                    F[e, j, i] = g[e, j, i]
+        return F
+
+    def _bc(self, helm, c, u, f, g, max_iter, tol):
+        sh = self.shape
+        F = self.bc_field(g)
+        b = self.gproj(f)
+
+        def op(v):
+            return self.apply_helmholtz(c, v) if helm else self.apply_laplace(v)
+        if self.neumann:
+            b = b + self.mask(self.global_sum(F))
+        else:
+            b = b - op(F)
+        x0 = self.mask(u)
+        x, r = krylov("minres" if helm else "pcg", lambda v: op(v.reshape(sh)).ravel(), b.ravel(), x0.ravel(),
+                      max_iter, tol, dot=lambda a, d: self.dot(a.reshape(sh), d.reshape(sh)))
+        x = self.unmask(x.reshape(sh))
+        if not self.neumann:
+            x = x + F
+        return x, r
+
+    def poisson_bc(self, u, f, g, max_iter, tol):
+        """Poisson with boundary data g (see bc_field), the composition of
+        sem_poisson_bc: Dirichlet by lifting, Neumann by the boundary
+        integral; returns the continuous solution and (success, n_iter,
+        residual)"""
+        return self._bc(False, None, u, f, g, max_iter, tol)
+
+    def helmholtz_bc(self, u, c, f, g, max_iter, tol):
+        return self._bc(True, c, u, f, g, max_iter, tol)

@@ -124,8 +124,10 @@ def lib():
         L.ref_helmholtz.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_double, _ip, _dp]
         L.ref_minres_res.argtypes = [C.c_void_p, _dp, C.c_double, _dp, _dp, _dp, _dp, C.c_int, C.c_double,
                                      _ip, _dp]
+        L.ref_pcg_laplace.argtypes = [C.c_void_p, _dp, _dp, C.c_int, C.c_double, _ip, _dp]
+        L.ref_minres_helmholtz.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_int, C.c_double, _ip, _dp]
         L.ref_schrodinger.argtypes = [C.c_void_p, C.c_int, _dp, _dp, _dp, C.c_double, C.c_int, C.c_double,
-                                      C.c_int, _dp, _ip]
+                                      C.c_int, C.c_int, C.c_double, _dp, _ip]
         lp = lapack_path()
         if lp is not None:
             L.ref_set_lapack(lp.encode())
@@ -280,6 +282,49 @@ class Mesh:
                                         C.byref(it), C.byref(res)), "helmholtz")
         return u, (bool(ok), int(it.value), float(res.value))
 
+    def pcg_laplace(self, x, b, max_iter, tol):
+        """the reference's pcg on Poisson's operator for a given b"""
+        x = _f(x).copy()
+        it, res = C.c_int(), C.c_double()
+        ok = _check(lib().ref_pcg_laplace(self._h, _p(x), _p(_f(b)), int(max_iter), float(tol), C.byref(it),
+                                          C.byref(res)), "pcg")
+        return x, (bool(ok), int(it.value), float(res.value))
+
+    def minres_helmholtz(self, c, x, b, max_iter, tol):
+        """the reference's minres on Helmholtz's operator for a given b"""
+        x = _f(x).copy()
+        it, res = C.c_int(), C.c_double()
+        ok = _check(lib().ref_minres_helmholtz(self._h, _p(_f(c)), _p(x), _p(_f(b)), int(max_iter), float(tol),
+                                               C.byref(it), C.byref(res)), "minres")
+        return x, (bool(ok), int(it.value), float(res.value))
+
+    def dirichlet_bc(self, helm, c, u, f, g, max_iter, tol):
+        """Inhomogeneous Dirichlet data by lifting, composed of the
+        reference's own gproj, galerkin operators, mask, unmask and
+        PCG/MINRES: u_D = g at every copy of a boundary node (0 elsewhere),
+        b = gproj(f) - A u_D, A u0 = b, u = unmask(u0) + u_D"""
+        X = self.zeros()
+        t, ptr, el, ii, jj = self.nodes()
+        E = self.edges()
+        g = _f(g)
+        N = self.N
+        k = np.arange(N)
+        sides = {1: (np.zeros(N, int), k), 2: (k, np.full(N, N - 1)), 3: (np.full(N, N - 1), k),
+                 4: (k, np.zeros(N, int))}  # reference side -> (j, i)
+        for row in E:
+            if row[6]:
+                e, s = int(row[0]), int(row[2])
+                j_, i_ = sides[s]
+                X[e, j_, i_] = g[e, j_, i_]
+        for n in range(self.n_nodes):
+            if t[n]:
+                for q in range(ptr[n], ptr[n + 1]):
+                    X[el[q], jj[q], ii[q]] = g[el[q], jj[q], ii[q]]
+        b = self.gproj(f) - (self.apply_helmholtz(c, X) if helm else self.apply_laplace(X))
+        x0 = self.mask(u)
+        x, r = self.minres_helmholtz(c, x0, b, max_iter, tol) if helm else self.pcg_laplace(x0, b, max_iter, tol)
+        return self.unmask(x) + X, r
+
     def minres_res(self, V, alpha, b_re, b_im, x_re, x_im, max_iter, tol):
         xr, xi = _f(x_re).copy(), _f(x_im).copy()
         it, res = C.c_int(), C.c_double()
@@ -288,13 +333,15 @@ class Mesh:
                     "minres")
         return xr, xi, (bool(ok), int(it.value), float(res.value))
 
-    def schrodinger(self, method: str, psi_re, psi_im, V, dt, max_iter, tol, n_steps):
-        """Run the reference's driver for exactly n_steps steps.  Returns
-        (re, im, success, steps_done, per-step wall seconds)."""
+    def schrodinger(self, method: str, psi_re, psi_im, V, dt, max_iter, tol, n_steps, untimed=0,
+                    budget_s=0.0):
+        """Run the reference's driver for n_steps steps (fewer once the steps
+        after the first ``untimed`` have taken ``budget_s`` seconds, when
+        given).  Returns (re, im, success, steps_done, per-step wall seconds)."""
         pr, pi = _f(psi_re).copy(), _f(psi_im).copy()
         times = np.zeros(max(int(n_steps), 1))
         done = C.c_int()
         ok = _check(lib().ref_schrodinger(self._h, METHODS[method], _p(pr), _p(pi), _p(_f(V)), float(dt),
-                                          int(max_iter), float(tol), int(n_steps), _p(times), C.byref(done)),
-                    "schrodinger")
+                                          int(max_iter), float(tol), int(n_steps), int(untimed), float(budget_s),
+                                          _p(times), C.byref(done)), "schrodinger")
         return pr, pi, bool(ok), int(done.value), times[: int(done.value)]

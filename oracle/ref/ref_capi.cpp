@@ -135,20 +135,27 @@ schro_omp::v_wrapper<real> make_pair_field(const Mesh<real>& m, const double* a,
 
 // Per-step callback of the drivers (include/openmp_impl/schrodinger.hpp:
 // 116-118): records the wall time of each step and stops after n steps, so
-// exactly n steps run whatever rounding does to the driver's t < T test.
+// exactly n steps run whatever rounding does to the driver's t < T test, or
+// earlier, once the steps after the first `untimed` have taken budget_s
+// seconds (budget_s <= 0: no budget).
 struct StepClock
 {
     int n_steps;
+    int untimed;
+    double budget_s;
     int* done;
     double* times;
+    double* spent;
     std::chrono::steady_clock::time_point* last;
     bool operator()(const field&, const field&)
     {
         auto now = std::chrono::steady_clock::now();
-        if (times) times[*done] = std::chrono::duration<double>(now - *last).count();
+        const double dt = std::chrono::duration<double>(now - *last).count();
+        if (times) times[*done] = dt;
+        if (*done >= untimed) *spent += dt;
         *last = now;
         ++*done;
-        return *done >= n_steps;
+        return *done >= n_steps || (budget_s > 0 && *done > untimed && *spent >= budget_s);
     }
 };
 
@@ -433,6 +440,63 @@ int ref_helmholtz(void* h, double* u, const double* c, const double* f, int maxi
     });
 }
 
+// The reference's PCG (include/pcg.hpp:59-97) on Poisson's operator and its
+// MINRES on Helmholtz's, with the drivers' dot product, for an arbitrary
+// right-hand side b (the drivers build b = gproj(f) themselves,
+// include/openmp_impl/poisson.hpp:20, helmholtz.hpp:21).  x in/out.
+int ref_pcg_laplace(void* h, double* x, const double* b, int maxit, double tol, int* n_iter, double* residual)
+{
+    return guarded([&] {
+        const auto& m = static_cast<RefMesh*>(h)->mesh;
+        schro_omp::solution_wrapper<real> xs(to_field(m, x)), bs(to_field(m, b));
+        auto op = [](field& v, const Mesh<real>& mesh) {
+#pragma omp parallel for if (v.size() > 63) schedule(static)
+            for (size_t i = 0; i < v.size(); ++i) v[i] = glaplace(v[i], mesh.elements[i], mesh.D, mesh.quadrature);
+        };
+        auto L = [&](const schro_omp::solution_wrapper<real>& v) {
+            return schro_omp::solution_wrapper<real>(schro_omp::galerkin_op<real>(op, v.values, m));
+        };
+        auto dotprod = [&](const schro_omp::solution_wrapper<real>& a, const schro_omp::solution_wrapper<real>& c) {
+            return schro_omp::dot<real>(m, a.values, c.values);
+        };
+        auto r = pcg<real>(xs, L, bs, dotprod, IdentityPreconditioner{}, maxit, tol);
+        from_field(xs.values, x);
+        *n_iter = r.n_iter;
+        *residual = r.residual;
+        return r.success ? 1 : 0;
+    });
+}
+
+int ref_minres_helmholtz(void* h, const double* c, double* x, const double* b, int maxit, double tol, int* n_iter,
+                         double* residual)
+{
+    return guarded([&] {
+        const auto& m = static_cast<RefMesh*>(h)->mesh;
+        field cf = to_field(m, c);
+        schro_omp::solution_wrapper<real> xs(to_field(m, x)), bs(to_field(m, b));
+        auto op = [&cf](field& v, const Mesh<real>& mesh) {
+            const auto& w = mesh.quadrature.w;
+#pragma omp parallel for if (v.size() > 63) schedule(static)
+            for (size_t i = 0; i < v.size(); ++i)
+            {
+                matrix<real> cuv = (arma::diagmat(w) * (v[i] % cf[i]) * arma::diagmat(w)) % mesh.elements[i].J;
+                v[i] = cuv + glaplace(v[i], mesh.elements[i], mesh.D, mesh.quadrature);
+            }
+        };
+        auto A = [&](const schro_omp::solution_wrapper<real>& v) {
+            return schro_omp::solution_wrapper<real>(schro_omp::galerkin_op<real>(op, v.values, m));
+        };
+        auto dotprod = [&](const schro_omp::solution_wrapper<real>& a, const schro_omp::solution_wrapper<real>& d) {
+            return schro_omp::dot<real>(m, a.values, d.values);
+        };
+        auto r = minres<real>(xs, A, bs, dotprod, IdentityPreconditioner{}, maxit, tol);
+        from_field(xs.values, x);
+        *n_iter = r.n_iter;
+        *residual = r.residual;
+        return r.success ? 1 : 0;
+    });
+}
+
 // The reference's MINRES (include/minres.hpp:19-107) on the Res operator
 // with the drivers' dot product (include/openmp_impl/schrodinger.hpp:
 // 368-371): x in/out
@@ -459,11 +523,12 @@ int ref_minres_res(void* h, const double* V, double alpha, const double* b0, con
 
 // The drivers schrodinger_bdf2 (method 0), schrodinger_dirk4s3 (1) and
 // schrodinger_dirk4s5 (2) (include/openmp_impl/schrodinger.hpp:22-128,
-// 138-285, 294-423), run for exactly n_steps steps of size dt through the
-// driver's callback.  step_times (n_steps entries, may be null) receives the
-// wall time of each step.  psi in/out.  Returns the driver's success flag.
+// 138-285, 294-423), run for n_steps steps of size dt through the driver's
+// callback, or fewer when the steps after the first `untimed` reach budget_s
+// seconds.  step_times (n_steps entries, may be null) receives the wall time
+// of each step.  psi in/out.  Returns the driver's success flag.
 int ref_schrodinger(void* h, int method, double* re, double* im, const double* V, double dt, int maxit,
-                    double tol, int n_steps, double* step_times, int* steps_done)
+                    double tol, int n_steps, int untimed, double budget_s, double* step_times, int* steps_done)
 {
     return guarded([&] {
         const auto& m = static_cast<RefMesh*>(h)->mesh;
@@ -474,8 +539,9 @@ int ref_schrodinger(void* h, int method, double* re, double* im, const double* V
         opts.dt = dt;
         opts.verbose = false;
         int done = 0;
+        double spent = 0.0;
         auto last = std::chrono::steady_clock::now();
-        StepClock cb{n_steps, &done, step_times, &last};
+        StepClock cb{n_steps, untimed, budget_s, &done, step_times, &spent, &last};
         // T past the last step: the callback ends the run after n_steps
         const real T = dt * (n_steps + 1);
         bool ok;

@@ -579,6 +579,15 @@ void or_global_sum(const or_mesh* m, double* a)
     }
 }
 
+/* Natural boundary: the boundary edges keep their single copy (unmask and
+ * global_sum already skip them, mask now does too) and every corner node
+ * is treated as interior (first copy owns, all copies summed). */
+void or_mesh_set_neumann(or_mesh* m)
+{
+    m->neumann = 1;
+    for (int c = 0; c < m->n_nodes; ++c) m->node_type[c] = OR_INTERIOR;
+}
+
 /* openmp_impl/mask.hpp:16-28, mask_side.hpp:12-52, mask_node.hpp:8-22 */
 void or_mask(const or_mesh* m, double* a)
 {
@@ -587,6 +596,7 @@ void or_mask(const or_mesh* m, double* a)
     for (int ed = 0; ed < m->n_edges; ++ed) {
         int e, s;
         if (m->edge_type[ed] == OR_BOUNDARY) {
+            if (m->neumann) continue;
             e = m->edge_el[2 * ed];
             s = m->edge_side[2 * ed];
         } else {

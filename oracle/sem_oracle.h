@@ -45,7 +45,13 @@ typedef struct or_mesh {
     int *node_el, *node_i, *node_j;
     /* metrics (include/Quad.hpp:17-21), [E][N][N] */
     double *J, *A, *B, *C;
+    /* natural boundary (no counterpart in the reference): boundary edges are
+     * not masked and boundary corners assemble like interior ones */
+    int neumann;
 } or_mesh;
+
+/* switch the mesh to the natural boundary */
+void or_mesh_set_neumann(or_mesh* m);
 
 /* a1: include/gauss_lobatto.hpp:43-126.  n = degree; x, w hold n+1 values.
  * Returns 0 on success. */

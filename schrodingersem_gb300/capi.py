@@ -84,6 +84,8 @@ SIGNATURES = {
     "sem_pcg_laplace": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_double, C.c_int, C.POINTER(SemSolverResults)]),
     "sem_poisson": (C.c_int, [_vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SemSolverResults)]),
     "sem_helmholtz": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SemSolverResults)]),
+    "sem_poisson_bc": (C.c_int, [_vp, _vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SemSolverResults)]),
+    "sem_helmholtz_bc": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, C.c_double, C.POINTER(SemSolverResults)]),
     "sem_schrodinger_bdf2": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(SemSolverOpts),
                                        STEP_CALLBACK, _vp, C.POINTER(C.c_int)]),
     "sem_schrodinger_dirk4s5": (C.c_int, [_vp, _vp, _vp, _vp, C.c_double, C.POINTER(SemSolverOpts),
@@ -122,6 +124,7 @@ SIGNATURES = {
 }
 
 SEM_FLAG_METRIC_CORRECTED = 0x1
+SEM_FLAG_NEUMANN = 0x2
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
 OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_EXTRAP_ORDER = 7, 8, 9, 10, 11
 OPT_ADAPTIVE_INNER = 12

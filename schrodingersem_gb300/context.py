@@ -47,11 +47,13 @@ def _ptr(a):
 
 class Context:
     def __init__(self, p: int, coords=None, elements=None, folder: str | None = None,
-                 corrected_metric: bool = False, stream=None):
+                 corrected_metric: bool = False, stream=None, neumann: bool = False):
         L = capi.load()
         self._L = L
         h = C.c_void_p()
-        flags = capi.SEM_FLAG_METRIC_CORRECTED if corrected_metric else 0
+        flags = (capi.SEM_FLAG_METRIC_CORRECTED if corrected_metric else 0) | \
+            (capi.SEM_FLAG_NEUMANN if neumann else 0)
+        self.neumann = bool(neumann)
         if folder is not None:
             check(L.sem_ctx_load(C.byref(h), int(p), folder.encode(), flags), "sem_ctx_load")
         else:
@@ -243,6 +245,21 @@ class Context:
         r = SemSolverResults()
         check(self._L.sem_helmholtz(self._h, _ptr(u), _ptr(c), _ptr(f), int(max_iter), float(tol), C.byref(r)),
               "sem_helmholtz")
+        return bool(r.success), int(r.n_iter), float(r.residual)
+
+    def poisson_bc(self, u, f, g, max_iter, tol):
+        """sem_poisson_bc: u (host or device) in/out, continuous on return;
+        g element-local (Dirichlet context) or (E, 4, N) normal derivatives
+        per side node (Neumann context)"""
+        r = SemSolverResults()
+        check(self._L.sem_poisson_bc(self._h, _ptr(u), _ptr(f), _ptr(g), int(max_iter), float(tol), C.byref(r)),
+              "sem_poisson_bc")
+        return bool(r.success), int(r.n_iter), float(r.residual)
+
+    def helmholtz_bc(self, u, c, f, g, max_iter, tol):
+        r = SemSolverResults()
+        check(self._L.sem_helmholtz_bc(self._h, _ptr(u), _ptr(c), _ptr(f), _ptr(g), int(max_iter), float(tol),
+                                       C.byref(r)), "sem_helmholtz_bc")
         return bool(r.success), int(r.n_iter), float(r.residual)
 
     def schrodinger_adaptive(self, psi_re, psi_im, V, T, dt0, max_iter, tol, err_tol, capacity=100000,

@@ -18,6 +18,7 @@
 #pragma once
 #include <cstdint>
 #include <cstring>
+#include <mutex>
 
 #include "sem_device.cuh"
 
@@ -656,26 +657,40 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
     if (threadIdx.x == 0) bulk_wait_all();
 }
 
-// grid of k_apply_bulk for one instantiation (occupancy queried once per process)
+// grid of k_apply_bulk for one instantiation.  The shared-memory opt-in is
+// a per-device attribute, so it is set, and the occupancy queried, once per
+// device (the current one, which owns the launch's stream), under a lock.
 template <int N, typename T, int OP, bool GATHER, bool MG>
 cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
                                  bool pair_asm, long long timeout_ns, cudaStream_t st)
 {
-    static int blocks_per_sm = -1, sms = 0;
+    constexpr int kMaxDev = 64;
+    static std::mutex mu;
+    static bool ready[kMaxDev] = {};
+    static int blocks_per_sm_of[kMaxDev] = {}, sms_of[kMaxDev] = {};
     constexpr size_t smem = bulk_smem_bytes<N, T, OP>();
     constexpr int TPB = bulk_tpb_k<T, OP, MG>();
-    if (blocks_per_sm < 0) {
-        cudaError_t e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER, MG>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        int dev = 0;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        int nb = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_apply_bulk<N, T, OP, GATHER, MG>, TPB, smem)) !=
-            cudaSuccess)
-            return e;
-        blocks_per_sm = nb;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDev) return cudaErrorInvalidDevice;
+    int blocks_per_sm = 0, sms = 0;
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        if (!ready[dev]) {
+            e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+            if (e != cudaSuccess) return e;
+            if ((e = cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+                return e;
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm_of[dev],
+                                                                   k_apply_bulk<N, T, OP, GATHER, MG>, TPB, smem)) !=
+                cudaSuccess)
+                return e;
+            ready[dev] = true;
+        }
+        blocks_per_sm = blocks_per_sm_of[dev];
+        sms = sms_of[dev];
     }
     if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
     if (!m.Dh) return cudaErrorInvalidValue;

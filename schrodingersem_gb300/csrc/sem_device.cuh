@@ -107,6 +107,12 @@ __device__ __forceinline__ bool ni_boundary(const NodeInfo& ni)
     return (ni.flags >> (12 + ni.sc)) & 1;
 }
 
+// a side copy with no partner (a side on a Neumann boundary)
+__device__ __forceinline__ bool ni_lone(const NodeInfo& ni)
+{
+    return ni.kind == 1 && ((ni.flags >> (16 + ni.sc)) & 1);
+}
+
 // flat index whose value unmask() copies into this node: the owner copy for
 // non-owner copies of interior sides/corners (unmask.hpp:12-36), else itself.
 __device__ __forceinline__ long long ni_gather_src(const DevMesh& m, const NodeInfo& ni, int e,
@@ -138,6 +144,7 @@ __device__ __forceinline__ T dss_value(const DevMesh& m, const T* Y, const NodeI
         const int sb = __ldg(m.side_base + 4 * e + ni.sc), ss = __ldg(m.side_step + 4 * e + ni.sc);
         if (ni_boundary(ni)) return MODE == DSS_SUM ? own : T(0);
         if (MODE == DSS_MASK && !ni_owner(ni)) return T(0);
+        if (ni_lone(ni)) return own;
         return own + ldcg(Y + ((long long)sb + (long long)ni.k * ss));  // owner + other in either copy: same bits
     }
     const int* cl = m.corner_nb + (size_t)(4 * e + ni.sc) * CORNER_NB_MAX;
@@ -454,7 +461,7 @@ __device__ __forceinline__ T nn_weight(const DevMesh& m, const NodeInfo& ni, int
     if (ni.kind == 0) return T(1);
     const int c4 = ni.kind == 2 ? __ldg(m.corner_cnt4 + e) : 0;
     if (ni_boundary(ni)) return T(0);
-    if (ni.kind == 1) return T(0.5);
+    if (ni.kind == 1) return ni_lone(ni) ? T(1) : T(0.5);
     return T(1) / T((c4 >> (8 * ni.sc)) & 255);
 }
 
@@ -668,7 +675,8 @@ __device__ __forceinline__ bool grid_barrier(GridSync* gs, long long timeout_ns)
             const unsigned long long t0 = global_ns();
             unsigned int polls = 0;
             while (((old ^ *vc) & 0x80000000u) == 0) {
-                if ((++polls & 63u) == 0) {
+                // the limit is checked on the first poll and every 64th after it
+                if ((++polls & 63u) == 1) {
                     if (*verr) break;
                     if ((long long)(global_ns() - t0) > timeout_ns) {
                         atomicExch(&gs->err, 1);

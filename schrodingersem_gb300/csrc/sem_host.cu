@@ -205,6 +205,7 @@ struct sem_ctx {
     std::vector<double> Drow_host;         // D row-major (DevMesh::Dh)
     std::vector<double> coords;            // [n_nodes][2]
     std::vector<int> elements;             // [E][4]
+    std::vector<int> fl_host;              // DevMesh::flags, host copy
     std::vector<double> J, A, B, C;        // host metrics [E][N][N]
     DevMesh dm;
     std::vector<void*> owned;              // device allocations freed at destroy
@@ -246,6 +247,8 @@ namespace semgb {
 const DevMesh& ctx_mesh(const sem_ctx* c) { return c->dm; }
 cudaStream_t ctx_stream(const sem_ctx* c) { return c->stream; }
 void ctx_count_launches(sem_ctx* c, long long k) { c->stats.kernel_launches += k; }
+int ctx_device(const sem_ctx* c) { return c->device; }
+void ctx_count_fp64_apply(sem_ctx* c) { c->stats.fp64_applies++; }
 int ctx_fail(int code, const char* msg) { return fail(code, msg); }
 }  // namespace semgb
 
@@ -374,6 +377,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
 {
     if (p < 1 || p > MAX_N - 1) return fail(SEM_ERR_ARG, "polynomial degree must be 1..16");
     if (n_nodes <= 0 || n_el <= 0 || !coords || !elements) return fail(SEM_ERR_ARG, "empty mesh");
+    if (flags & ~(SEM_FLAG_METRIC_CORRECTED | SEM_FLAG_NEUMANN)) return fail(SEM_ERR_ARG, "unknown context flag");
     const int N = p + 1, NN = N * N;
     if ((long long)n_el * NN >= (1LL << 31)) return fail(SEM_ERR_UNSUPPORTED, "mesh too large for 32-bit node indices");
     c->p = p;
@@ -421,8 +425,11 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             }
         }
     c->n_edges = (int)edges.size();
+    // Neumann context: boundary sides are owned and partnerless, boundary
+    // corners ordinary (node_bnd stays clear); on_bnd marks them for the count
+    const bool neumann = (flags & SEM_FLAG_NEUMANN) != 0;
     std::vector<int> fl(n_el, 0), sbase(4 * (size_t)n_el, -1), sstep(4 * (size_t)n_el, 0);
-    std::vector<char> node_bnd(n_nodes, 0);
+    std::vector<char> node_bnd(n_nodes, 0), on_bnd(n_nodes, 0);
     auto side_pos = [&](int e, int s, int k) -> long long {  // flat index of node k on side s
         const long long b = (long long)e * NN;
         switch (s) {
@@ -436,6 +443,12 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         const Ed& ed = edges[q];
         if (ed.el[1] < 0) {
             ++c->n_bnd_edges;
+            on_bnd[elements[4 * ed.el[0] + emap1[ed.side[0]]]] = 1;
+            on_bnd[elements[4 * ed.el[0] + emap2[ed.side[0]]]] = 1;
+            if (neumann) {
+                fl[ed.el[0]] |= (1 << ed.side[0]) | (65536 << ed.side[0]);
+                continue;
+            }
             fl[ed.el[0]] |= (1 << ed.side[0]) | (16 << ed.side[0]);
             node_bnd[elements[4 * ed.el[0] + emap1[ed.side[0]]]] = 1;
             node_bnd[elements[4 * ed.el[0] + emap2[ed.side[0]]]] = 1;
@@ -478,7 +491,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             if (nflat[nptr[node]] == flat) fl[e] |= (256 << cc);
             if (node_bnd[node]) fl[e] |= (4096 << cc);
         }
-    for (int k = 0; k < n_nodes; ++k) c->n_bnd_nodes += node_bnd[k];
+    for (int k = 0; k < n_nodes; ++k) c->n_bnd_nodes += on_bnd[k];
     // corner copies in CSR order per element corner (the gathers read them
     // with one dependent load instead of three)
     std::vector<int> corner_nb((size_t)n_el * 4 * CORNER_NB_MAX, -1), corner_cnt4(n_el, 0);
@@ -537,11 +550,11 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             ring_src[(size_t)e * R + r] = src;
         }
         for (int sd = 0; sd < 4; ++sd) {
-            const bool bnd = fl[e] & (16 << sd), own = fl[e] & (1 << sd);
+            const bool bnd = fl[e] & (16 << sd), own = fl[e] & (1 << sd), lone = fl[e] & (65536 << sd);
             for (int k = 1; k < N - 1; ++k) {
                 if (bnd)
                     bnd_flat.push_back((int)side_pos(e, sd, k));
-                else if (own)
+                else if (own && !lone)
                     edge_pairs.push_back(
                         make_int2((int)side_pos(e, sd, k), (int)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd])));
             }
@@ -647,7 +660,8 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
                     } else if (ib || jb) {
                         const int sd = jb ? (j == 0 ? 0 : 2) : (i == N - 1 ? 1 : 3);
                         const int k = jb ? i : j;
-                        if (!(fl[e] & (16 << sd))) v += loc[(size_t)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd])];
+                        if (!(fl[e] & ((16 | 65536) << sd)))
+                            v += loc[(size_t)(sbase[4 * e + sd] + (long long)k * sstep[4 * e + sd])];
                     }
                     out[f] = v;
                 }
@@ -670,6 +684,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         fel[e] = make_float4((float)(ax * ay), (float)(ay / ax), (float)(ax / ay), 0.f);
     }
 
+    c->fl_host = fl;
     // device copies
     DevMesh& d = c->dm;
     d.N = N;
@@ -1469,6 +1484,117 @@ extern "C" int sem_helmholtz(sem_ctx* c, double* u, const double* cf, const doub
     return SEM_OK;
 }
 
+// --------------------------------------------- boundary data (no counterpart)
+// Element-local field built from the boundary data g (host or device):
+// Dirichlet context, g is an element-local field and the result the lifting
+// u_D (g at every copy of a boundary node, 0 elsewhere); Neumann context, g
+// holds du/dn per element side node ([E][4][N], side s as in DevMesh::flags,
+// node k along the side in the element's own direction) and the result is
+// the boundary integral of g against each basis function, w_k (L/2) g_k at
+// node k of every boundary side of length L (GLL quadrature on the straight
+// side), a corner copy collecting the terms of each of its element's
+// boundary sides that meet there.  Written to dev.
+static int bc_field(sem_ctx* c, const double* g, double* dev)
+{
+    const int N = c->N, NN = N * N;
+    const bool neumann = (c->flags & SEM_FLAG_NEUMANN) != 0;
+    const size_t ng = neumann ? (size_t)c->E * 4 * N : (size_t)c->n;
+    std::vector<double> gh(ng), F((size_t)c->n, 0.0);
+    if (is_device_ptr(g)) {
+        SEM_CUDA(cudaMemcpyAsync(gh.data(), g, sizeof(double) * ng, cudaMemcpyDeviceToHost, c->stream));
+        SEM_CUDA(cudaStreamSynchronize(c->stream));
+    } else {
+        std::copy(g, g + ng, gh.begin());
+    }
+    static const int ca[] = {0, 1, 3, 0}, cb[] = {1, 2, 2, 3};  // corners of side s, k = 0 at ca
+    auto flat_of = [&](int e, int s, int k) -> size_t {
+        const size_t b = (size_t)e * NN;
+        switch (s) {
+            case 0: return b + k;
+            case 1: return b + (N - 1) + (size_t)k * N;
+            case 2: return b + k + (size_t)(N - 1) * N;
+            default: return b + (size_t)k * N;
+        }
+    };
+    for (int e = 0; e < c->E; ++e) {
+        const int fe = c->fl_host[e];
+        for (int sd = 0; sd < 4; ++sd) {
+            if (!(fe & ((neumann ? 65536 : 16) << sd))) continue;
+            if (!neumann) {
+                for (int k = 0; k < N; ++k) F[flat_of(e, sd, k)] = gh[flat_of(e, sd, k)];
+                continue;
+            }
+            const int a = c->elements[4 * (size_t)e + ca[sd]], b = c->elements[4 * (size_t)e + cb[sd]];
+            const double half = 0.5 * std::hypot(c->coords[2 * (size_t)b] - c->coords[2 * (size_t)a],
+                                                 c->coords[2 * (size_t)b + 1] - c->coords[2 * (size_t)a + 1]);
+            for (int k = 0; k < N; ++k) F[flat_of(e, sd, k)] += c->w[k] * half * gh[((size_t)e * 4 + sd) * N + k];
+        }
+        if (!neumann) {  // copies of boundary corner nodes whose sides are interior
+            for (int cc = 0; cc < 4; ++cc)
+                if (fe & (4096 << cc)) {
+                    const size_t f = (size_t)e * NN + (cc == 1 || cc == 2 ? N - 1 : 0) +
+                                     (cc >= 2 ? (size_t)(N - 1) * N : 0);
+                    F[f] = gh[f];
+                }
+        }
+    }
+    SEM_CUDA(cudaMemcpyAsync(dev, F.data(), sizeof(double) * c->n, cudaMemcpyHostToDevice, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    return SEM_OK;
+}
+
+static int bc_solve(sem_ctx* c, bool helm, double* u, const double* cf, const double* f, const double* g,
+                    int max_iter, double tol, sem_solver_results* res)
+{
+    SEM_CHECK_CTX(c);
+    if (!u || !f || !g || !res || (helm && !cf)) return fail(SEM_ERR_ARG, "null argument");
+    bool uh = false, fh = false, ch = false;
+    const double *fd = nullptr, *cd = nullptr, *ud0 = nullptr;
+    int s = 0;
+    if ((s = stage_in(c, "drv_f", f, c->n, &fd, &fh))) return s;
+    if (helm && (s = stage_in(c, "drv_c", cf, c->n, &cd, &ch))) return s;
+    if ((s = stage_in(c, "drv_u", u, c->n, &ud0, &uh))) return s;
+    double* ud = const_cast<double*>(ud0);
+    double *b = nullptr, *F = nullptr, *T = nullptr;
+    if ((s = wsget(c, "drv_b", c->n, &b)) || (s = wsget(c, "bc_F", c->n, &F)) || (s = wsget(c, "bc_T", c->n, &T)))
+        return s;
+    if ((s = bc_field(c, g, F))) return s;
+    if ((s = sem_gproj(c, fd, b))) return s;
+    const bool neumann = (c->flags & SEM_FLAG_NEUMANN) != 0;
+    if (!neumann) {  // b -= A u_D (masked rows: the interior equations)
+        if ((s = apply_galerkin(c, helm ? OP_HELM : OP_LAPLACE, cd, 0.0, F, nullptr, T, nullptr))) return s;
+    } else {  // b += the assembled boundary integral
+        SEM_CUDA(cudaMemcpyAsync(T, F, sizeof(double) * c->n, cudaMemcpyDeviceToDevice, c->stream));
+        if ((s = sem_global_sum(c, T)) || (s = sem_mask(c, T))) return s;
+    }
+    if ((s = sem_vec_axpby(c, c->n, 1.0, b, neumann ? 1.0 : -1.0, T, b))) return s;
+    if ((s = sem_mask(c, ud))) return s;  // the guess of the interior part
+    if (helm) {
+        if ((s = sem_minres_helmholtz(c, cd, ud, b, max_iter, tol, 0, res))) return s;
+    } else {
+        if ((s = sem_pcg_laplace(c, ud, b, max_iter, tol, 0, res))) return s;
+    }
+    if ((s = sem_unmask(c, ud))) return s;
+    if (!neumann && (s = sem_vec_axpby(c, c->n, 1.0, ud, 1.0, F, ud))) return s;  // u = u0 + u_D
+    if (uh) {
+        SEM_CUDA(cudaMemcpyAsync(u, ud, sizeof(double) * c->n, cudaMemcpyDeviceToHost, c->stream));
+        SEM_CUDA(cudaStreamSynchronize(c->stream));
+    }
+    return SEM_OK;
+}
+
+extern "C" int sem_poisson_bc(sem_ctx* c, double* u, const double* f, const double* g, int max_iter, double tol,
+                              sem_solver_results* res)
+{
+    return bc_solve(c, false, u, nullptr, f, g, max_iter, tol, res);
+}
+
+extern "C" int sem_helmholtz_bc(sem_ctx* c, double* u, const double* cf, const double* f, const double* g,
+                                int max_iter, double tol, sem_solver_results* res)
+{
+    return bc_solve(c, true, u, cf, f, g, max_iter, tol, res);
+}
+
 // state shared by the three Schroedinger drivers
 struct SchroRun {
     sem_ctx* c;
@@ -1728,6 +1854,9 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
 {
     SEM_CHECK_CTX(c);
     if (!psi_re || !psi_im || !V || !o || !success) return fail(SEM_ERR_ARG, "null argument");
+    // the reference loops while t < T with t += dt (schrodinger.hpp:219,268,
+    // 376,406): a step that is not positive would never end the run
+    if (!(o->dt > 0)) return fail(SEM_ERR_ARG, "dt must be positive");
     SchroRun r{};
     int s = schro_begin(c, psi_re, psi_im, V, &r);
     if (s) return s;
@@ -2048,6 +2177,8 @@ extern "C" int sem_schrodinger_bdf2(sem_ctx* c, double* psi_re, double* psi_im, 
 {
     SEM_CHECK_CTX(c);
     if (!psi_re || !psi_im || !V || !o || !success) return fail(SEM_ERR_ARG, "null argument");
+    // the reference loops while t < T with t += dt (schrodinger.hpp:89,107)
+    if (!(o->dt > 0)) return fail(SEM_ERR_ARG, "dt must be positive");
     SchroRun r{};
     int s = schro_begin(c, psi_re, psi_im, V, &r);
     if (s) return s;

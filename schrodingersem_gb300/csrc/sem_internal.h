@@ -33,7 +33,10 @@ enum DssMode : int {
 //  bits 0-3   side s owned by this element (it is Edge::elements[0])
 //  bits 4-7   side s on the boundary
 //  bits 8-11  corner c owned (first of CornerNode::connected_elements)
-//  bits 12-15 corner c on the boundary
+//  bits 12-15 corner c on the (Dirichlet) boundary
+//  bits 16-19 side s on a Neumann boundary: owned, no partner copy (a Neumann
+//             context leaves the boundary bits clear; its boundary corners
+//             assemble over their copies like interior corners)
 // Sides s = 0..3 are the reference's sides 1..4: j=0, i=N-1, j=N-1, i=0.
 // Corners c = 0..3 are (0,0), (N-1,0), (N-1,N-1), (0,N-1).
 
@@ -244,6 +247,8 @@ namespace semgb {
 const DevMesh& ctx_mesh(const sem_ctx* c);
 cudaStream_t ctx_stream(const sem_ctx* c);
 void ctx_count_launches(sem_ctx* c, long long k);
+int ctx_device(const sem_ctx* c);     // ordinal of the device the context was created on
+void ctx_count_fp64_apply(sem_ctx* c);  // one more FP64 operator apply in sem_stats
 int ctx_fail(int code, const char* msg);  // records the message, returns code
 }  // namespace semgb
 

@@ -33,21 +33,19 @@ __device__ __align__(256) double g_noalloc_scratch[kNoAllocScratchValues];
 // Device address of g_noalloc_scratch per device, filled on the first call
 // made on that device.  In host code the symbol g_noalloc_scratch is only a
 // host-side stand-in: its address must come from cudaGetSymbolAddress with
-// the device current.
+// that device current.  The entry point runs only with the context's own
+// device current (it rejects other calls), so the lookup is for that device.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 double* g_scratch_ptr[kMaxDevices] = {};
 
-int scratch_for_current_device(double** out)
+int scratch_for_device(int dev, double** out)
 {
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return ctx_fail(SEM_ERR_CUDA, cudaGetErrorString(e));
     if (dev < 0 || dev >= kMaxDevices) return ctx_fail(SEM_ERR_UNSUPPORTED, "device ordinal above 63");
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_scratch_ptr[dev]) {
         void* p = nullptr;
-        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             std::string msg = std::string("cudaGetSymbolAddress(noalloc scratch): ") + cudaGetErrorString(e);
             return ctx_fail(SEM_ERR_CUDA, msg.c_str());
@@ -84,8 +82,14 @@ extern "C" int sem_apply_schro_res_noalloc(sem_ctx* c, const double* V, double a
                           std::to_string(kNoAllocScratchValues) + "; use sem_apply_schro_res";
         return ctx_fail(SEM_ERR_UNSUPPORTED, msg.c_str());
     }
+    // the context's stream and the scratch belong to the context's device
+    int cur = -1;
+    cudaError_t ge = cudaGetDevice(&cur);
+    if (ge != cudaSuccess) return ctx_fail(SEM_ERR_CUDA, cudaGetErrorString(ge));
+    if (cur != ctx_device(c))
+        return ctx_fail(SEM_ERR_ARG, "sem_apply_schro_res_noalloc: make the context's device current first");
     double* Y = nullptr;
-    int s = scratch_for_current_device(&Y);
+    int s = scratch_for_device(cur, &Y);
     if (s) return s;
     double* Y1 = Y + m.n;
     cudaStream_t st = ctx_stream(c);
@@ -107,5 +111,6 @@ extern "C" int sem_apply_schro_res_noalloc(sem_ctx* c, const double* V, double a
         return ctx_fail(SEM_ERR_CUDA, msg.c_str());
     }
     ctx_count_launches(c, 3);
+    ctx_count_fp64_apply(c);
     return SEM_OK;
 }

@@ -25,6 +25,9 @@ Cases (``tests/util.py`` REF_MESHES names the synthetic meshes):
       0.15h (seed 0), p = 4, f = 2 pi^2 sin(pi x) sin(pi y), PCG to 1e-12
   reftests  the reference's own integration tests (tests/poisson.cpp,
       helmholtz.cpp, schrodinger.cpp) with their outputs and iteration counts
+  bc_dirichlet  inhomogeneous Dirichlet data on the sample mesh, p = 6, by
+      lifting composed of the reference's own gproj, galerkin operators,
+      mask/unmask and PCG (Poisson) / MINRES (Helmholtz) to 1e-12
 """
 import os
 import sys
@@ -152,6 +155,19 @@ def main(reference: str) -> None:
         assert ok and done == 10
         out[f"schro_{meth}_re"], out[f"schro_{meth}_im"] = pr, pi
     save("reftests", out)
+
+    # inhomogeneous Dirichlet data by lifting
+    m = R.Mesh(6, folders["small"])
+    X, Y = m.node_coords()
+    g = np.exp(X) * np.sin(Y)
+    f = np.cos(X) * Y
+    c = 1.0 + 0.5 * np.sin(X)
+    up, (okp, itp, rp) = m.dirichlet_bc(False, None, m.zeros(), f, g, m.dof(), 1e-12)
+    uh, (okh, ith, rh) = m.dirichlet_bc(True, c, m.zeros(), f, g, 10 * m.dof(), 1e-12)
+    assert okp and okh
+    save("bc_dirichlet", {"p": np.array(6), "g": g, "f": f, "c": c, "poisson_u": up, "poisson_iters": np.array(itp),
+                          "poisson_residual": np.array(rp), "helmholtz_u": uh, "helmholtz_iters": np.array(ith),
+                          "helmholtz_residual": np.array(rh), "tol": np.array(1e-12)})
 
 
 if __name__ == "__main__":

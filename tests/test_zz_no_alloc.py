@@ -62,3 +62,41 @@ def test_noalloc_rejects_meshes_above_capacity(semlib):
     st = L.sem_apply_schro_res_noalloc(ctx._h, p, 0.1, p, p, p, p)
     assert st == 6  # SEM_ERR_UNSUPPORTED
     assert b"static capacity" in L.sem_last_error()
+
+
+def test_noalloc_in_place_and_allocates_nothing(semlib):
+    """Outputs aliasing the inputs (the case where the allocating call needs
+    its workspace) give the allocating call's result; after the first call
+    on the device (which may load the library's device code and its static
+    array), further calls leave the device's free memory unchanged; each
+    call counts one FP64 apply."""
+    import torch
+
+    from schrodingersem_gb300 import capi
+    L = capi.load()
+    co, el = structured(10, box=(-2.0, 2.0, -2.0, 2.0), jitter=0.15, seed=9)
+    ctx = semlib.Context(6, coords=co, elements=el)
+    h = ctx._h
+    g = torch.Generator(device="cuda").manual_seed(5)
+    V = torch.rand(ctx.shape, dtype=torch.float64, device="cuda", generator=g) * 4 - 2
+    qr = torch.randn(ctx.shape, dtype=torch.float64, device="cuda", generator=g)
+    qi = torch.randn(ctx.shape, dtype=torch.float64, device="cuda", generator=g)
+    p = lambda t: C.c_void_p(t.data_ptr())  # noqa: E731
+    ar, ai = qr.clone(), qi.clone()
+    capi.check(L.sem_apply_schro_res(h, p(V), 0.02, p(ar), p(ai), p(ar), p(ai)), "sem_apply_schro_res")
+    free = []
+    for call in range(3):
+        br, bi = qr.clone(), qi.clone()
+        before = ctx.stats().fp64_applies
+        capi.check(L.sem_apply_schro_res_noalloc(h, p(V), 0.02, p(br), p(bi), p(br), p(bi)),
+                   "sem_apply_schro_res_noalloc")
+        torch.cuda.synchronize()
+        assert ctx.stats().fp64_applies == before + 1
+        free.append(torch.cuda.mem_get_info()[0])
+        for x, y in ((br, ar), (bi, ai)):
+            assert _rel(x.cpu().numpy(), y.cpu().numpy()) <= TOL64
+        del br, bi
+        torch.cuda.synchronize()
+    # the clones are freed to torch's cache, not to the device, so any drop
+    # in free memory after the first call would be the entry point's own
+    assert free[1] == free[2], free
