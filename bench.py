@@ -398,40 +398,63 @@ def batch_fields(S, torch, insts):
     return re, im, V
 
 
-def run_batch(n_instances=1024, steps=100, warmup=3, seed=2026):
+def run_batch(n_instances=1024, steps=100, warmup=3, seed=2026, rank=0, world=1, dist=None):
     """the seeded ensemble: BDF2 dt = 5e-3, MINRES 1e-10, FP32 inner + FP64
     refinement, element preconditioner; warm-up steps capture the graph,
-    then `steps` timed steps of all instances (device time of the replays)"""
+    then `steps` timed steps of all instances (device time of the replays).
+    With world > 1 every rank runs its share of the instances
+    (schrodingersem_gb300.ensemble.shard), the time is the max over ranks
+    and the per-instance results are gathered to rank 0 (None elsewhere)."""
     import torch
 
     import schrodingersem_gb300 as S
     from schrodingersem_gb300 import capi
+    from schrodingersem_gb300 import ensemble as ens
     from schrodingersem_gb300.batch import Batch
     insts = make_instances(n_instances, seed)
+    costs = [ens.instance_cost(i["n"] ** 2, i["p"]) for i in insts]
+    mine = ens.shard(costs, world)[rank]
+    my_insts = [insts[k] for k in mine]
     t0 = time.time()
-    B = Batch([(i["p"], i["coords"], i["elements"]) for i in insts])
+    B = Batch([(i["p"], i["coords"], i["elements"]) for i in my_insts])
     setup_s = time.time() - t0
     B.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
-    re, im, V = batch_fields(S, torch, insts)
+    re, im, V = batch_fields(S, torch, my_insts)
     dt, maxit = 2.5e-3, 200000  # dt' = dt/2 of the workload's 5e-3
     B.bdf2(re, im, V, (warmup - 0.5) * dt, dt, maxit, 1e-10)
     s0 = B.stats()
     torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
     t0 = time.time()
     ok = B.bdf2(re, im, V, (steps - 0.5) * dt, dt, maxit, 1e-10)
     torch.cuda.synchronize()
     wall = time.time() - t0
     s1 = B.stats()
     ms = s1.kernel_ms - s0.kernel_ms
+    its = s1.krylov_iterations - s0.krylov_iterations
+    kmax = {p: s1.kmax_of_p[p] for p in (4, 6, 8)}
+    local = {k: bool(ok[q]) for q, k in enumerate(mine)}
+    if dist:
+        t = torch.tensor([ms, wall, float(its)], device="cuda", dtype=torch.float64)
+        tmax = t.clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms, wall, its = float(tmax[0]), float(tmax[1]), float(t[2])
+    conv = ens.gather_results(local, n_instances, rank, world, dist)
+    if rank != 0:
+        return None
     nodes = sum(i["n"] ** 2 * (i["p"] + 1) ** 2 for i in insts)
     return {
         "metric": "batched BDF2 instance-steps per second", "value": n_instances * steps / (ms / 1e3),
         "unit": "instance-steps/s", "instances": n_instances, "steps": steps, "warmup": warmup,
         "ms_per_step": ms / steps, "wall_s": wall, "setup_s": setup_s,
-        "local_nodes_per_component": nodes, "converged": int(sum(ok)),
-        "inner_iterations_per_instance_step": (s1.krylov_iterations - s0.krylov_iterations) / (n_instances * steps),
+        "local_nodes_per_component": nodes, "converged": int(sum(conv)),
+        "inner_iterations_per_instance_step": its / (n_instances * steps),
         "graph_launches": s1.graph_launches - s0.graph_launches, "graphs_built": s1.graphs_built,
-        "kmax_of_p": {p: s1.kmax_of_p[p] for p in (4, 6, 8)},
+        "kmax_of_p": kmax, "ranks": world,
+        "sharding": ("instances partitioned across ranks by cost, no data-path collective; time = max over "
+                     "ranks" if world > 1 else "one rank"),
         "config": {"workload": f"{n_instances:,} seeded instances: n~U{{4..32}} quads on [-6,6]^2, p in {{4,6,8}}, "
                                "6-Gaussian potentials, Gaussian packets; BDF2 dt=5e-3, MINRES 1e-10, FP32 inner + "
                                "FP64 refinement, element preconditioner", "dtype": "f64+f32"},
@@ -680,6 +703,7 @@ def run_form(ctx, torch, form, re, im, Vr, steps, warmup, flush, check_steps):
         "it64": s1.solver_iterations_fp64 - s0.solver_iterations_fp64,
         "it32": s1.solver_iterations_fp32 - s0.solver_iterations_fp32,
         "applies64": s1.fp64_applies - s0.fp64_applies,
+        "resident_launches": s1.resident_launches - s0.resident_launches,
         "learned": ({"guesses": s1.learned_guesses - s0.learned_guesses,
                      "accepted": s1.learned_accepted - s0.learned_accepted,
                      "last_residual_ratio": s1.last_guess_residual_ratio, "last_theta": s1.last_guess_theta,
@@ -815,6 +839,9 @@ def run_ours(args):
         e2e_times.append(e0.elapsed_time(e1))
     e2e_s = float(np.mean(e2e_times)) / 1e3
     nbytes = ctx.n * 8
+    # ensemble leg: every rank advances its share of the instances
+    batch = run_batch(1024, steps=args.batch_steps, warmup=2, rank=rank, world=world, dist=dist) \
+        if args.batch_steps > 0 else None
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -836,7 +863,9 @@ def run_ours(args):
     sweeps_total = H["applies64"] if prec == "mixed" else 0
     alg_bytes = H["it64"] * b64 + H["it32"] * b32 + sweeps_total * n * 8 * 14
     achieved = alg_bytes / (H["solver_ms"] / 1e3) / 1e9 if H["solver_ms"] > 0 else None
-    kern = "k_minres_mixed<9,RES>" if prec == "mixed" else "k_minres<9,double,RES>"
+    resident = H["resident_launches"] > 0
+    kern = ("k_minres_resident<9>" if resident else "k_minres_mixed<9,RES>") if prec == "mixed" \
+        else "k_minres<9,double,RES>"
     it_total = H["it32"] + H["it64"]
     us_per_it = 1e3 * H["solver_ms"] / it_total if it_total else None
     forms_out = {f: {"s_per_step": r["ms"] / 1e3, "minres_tol": r["tol"],
@@ -848,7 +877,6 @@ def run_ours(args):
     ref_iters = res["fp64_reftol"]["iters_per_step"] if "fp64_reftol" in res else \
         (res["fp64"]["iters_per_step"] if "fp64" in res else H["iters_per_step"])
     cpu = cpu_step_sample(ref_iters) if not args.no_cpu else None
-    batch = run_batch(1024, steps=args.batch_steps, warmup=2) if args.batch_steps > 0 else None
     if batch and not args.no_cpu:
         batch["cpu_baseline"] = batch_cpu_baseline(1024)
         batch["speedup_vs_cpu"] = batch["value"] / batch["cpu_baseline"]["value"]
@@ -877,14 +905,18 @@ def run_ours(args):
                      "kernel": kern + " (persistent cooperative solver)",
                      "algorithmic_bytes": alg_bytes, "fp64_iterations": H["it64"], "fp32_iterations": H["it32"],
                      "kernel_ms": H["solver_ms"], "peak_source": peak_src,
-                     "limiter": "latency: the working set (~40 MB) stays in L2; grid barriers and dependent "
-                                "L2 round trips set the time per iteration",
+                     "limiter": ("latency: the inner Krylov vectors stay in shared memory and registers "
+                                 "(only element-ring copies and the FP64 refinement touch global memory); "
+                                 "per iteration two grid all-reduces, two ring gathers from L2 and the "
+                                 "on-chip element passes" if resident else
+                                 "latency: the working set (~40 MB) stays in L2; grid barriers and dependent "
+                                 "L2 round trips set the time per iteration"),
                      "latency_model": {"us_per_iteration": us_per_it,
                                        "floor_us_per_iteration": floor_us,
                                        "floor_case": "same kernel and grid, 12x12 quads p=8 (one element per "
                                                      "block): barriers + scalar step + pass latencies",
                                        "algorithmic_bytes_per_iteration": b32,
-                                       "l2_gbs_at_measured_rate": (b32 / (us_per_it * 1e-6) / 1e9)
+                                       "algorithmic_gbs_at_measured_rate": (b32 / (us_per_it * 1e-6) / 1e9)
                                        if us_per_it else None}},
         "apply": ({"fp32_gbs": app["fp32"]["gbs"], "fp32_frac_hbm": app["fp32"]["frac_hbm"],
                    "fp64_gbs": app["fp64"]["gbs"], "fp64_tflops": app["fp64"]["tflops"],

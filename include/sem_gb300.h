@@ -82,6 +82,12 @@ enum sem_option {
     SEM_OPT_ADAPTIVE_INNER = 12, /* mixed mode: 1 (default) a sweep's inner tolerance is relaxed
                                     to what the outer test still needs (x 0.3), 0 always
                                     SEM_OPT_INNER_TOL */
+    SEM_OPT_RESIDENT = 13,       /* mixed mode, Res with SEM_PRECOND_FDM: 1 (default) keep the
+                                    FP32 inner solve's vectors on chip (shared memory and
+                                    registers; only element-ring copies are exchanged through
+                                    global memory) when each SM's share of the mesh fits
+                                    (p = 4, 6, 8, 10; up to 31 elements per SM at p = 8);
+                                    0 always the staged kernel.  Same FP64 stopping test */
     SEM_OPT_EXTRAP_ORDER = 11,   /* stage guess of SEM_GUESS_EXTRAPOLATE / _LEARNED: 1 (default)
                                     linear 2 z1 - z2, 2 quadratic 3 z1 - 3 z2 + z3 once three
                                     previous steps exist */
@@ -140,6 +146,8 @@ typedef struct {
     double last_guess_residual_ratio; /* |r(guess used)| / |r(extrapolated)| of the last such stage */
     double last_guess_theta;        /* step taken along the predicted correction (1: as predicted) */
     double learned_ratio_sum;       /* sum of |r(guess used)| / |r(extrapolated)| over learned guesses */
+    long long resident_launches;    /* persistent solver launches with the on-chip inner solve
+                                       (SEM_OPT_RESIDENT) */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop

@@ -39,7 +39,8 @@ class SemStats(C.Structure):
                 ("solver_kernel_ms", C.c_double), ("solver_iterations_fp64", C.c_longlong),
                 ("solver_iterations_fp32", C.c_longlong), ("learned_guesses", C.c_longlong),
                 ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double),
-                ("last_guess_theta", C.c_double), ("learned_ratio_sum", C.c_double)]
+                ("last_guess_theta", C.c_double), ("learned_ratio_sum", C.c_double),
+                ("resident_launches", C.c_longlong)]
 
 
 class SemBatchStats(C.Structure):
@@ -128,6 +129,7 @@ SEM_FLAG_NEUMANN = 0x2
 OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MAX_REFINE, OPT_PROFILE = 1, 2, 3, 4, 5, 6
 OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_EXTRAP_ORDER = 7, 8, 9, 10, 11
 OPT_ADAPTIVE_INNER = 12
+OPT_RESIDENT = 13
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

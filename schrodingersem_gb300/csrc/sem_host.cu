@@ -35,6 +35,19 @@ static int fail(int code, const std::string& msg)
             return fail(SEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// the degrees with an on-chip resident inner solver (sem_resident.cu)
+template <class F>
+static bool dispatch_resident(int N, F&& f)
+{
+    switch (N) {
+        case 5: f(std::integral_constant<int, 5>{}); return true;
+        case 7: f(std::integral_constant<int, 7>{}); return true;
+        case 9: f(std::integral_constant<int, 9>{}); return true;
+        case 11: f(std::integral_constant<int, 11>{}); return true;
+        default: return false;
+    }
+}
+
 template <class F>
 static cudaError_t dispatch_n(int N, F&& f)
 {
@@ -79,6 +92,9 @@ static int grid_1d(long long n) { return (int)std::min<long long>((n + 255) / 25
 
 // dynamic shared memory a persistent solver block may use for staging
 static const size_t kSolverSmemBudget = 160 * 1024;
+// the resident inner solve may use all of an SM's shared memory (227 KB per
+// block, less the kernel's static arrays)
+static const size_t kResidentSmemBudget = 227 * 1024 - 512;
 
 // Diagonal preconditioner P^-1 (continuous format).  Res = [M, aL; aL, -M]:
 // P = diag(d, d), d = sqrt(m^2 + a^2 (k + m V)^2), the diagonal of |Res|
@@ -203,6 +219,7 @@ struct sem_ctx {
     unsigned flags = 0;
     std::vector<double> x, w, D;           // D column-major
     std::vector<double> Drow_host;         // D row-major (DevMesh::Dh)
+    std::vector<float> D32_host, S32_host; // FP32 D and preconditioner basis S, row-major
     std::vector<double> coords;            // [n_nodes][2]
     std::vector<int> elements;             // [E][4]
     std::vector<int> fl_host;              // DevMesh::flags, host copy
@@ -224,6 +241,7 @@ struct sem_ctx {
     int apply_pipeline = 1;
     int extrap_order = 1;
     int adaptive_inner = 1;
+    int resident = 1;
     // stage-guess history of the SDIRK drivers (persists across calls)
     long long hist_steps = 0;
     int hist_stages = 0;
@@ -705,6 +723,8 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
         return f;
     };
+    c->D32_host = Drowf;
+    c->S32_host = tof(fS);
     int s = 0;
     if ((s = upload(c, fl, &d.flags)) || (s = upload(c, sbase, &d.side_base)) ||
         (s = upload(c, sstep, &d.side_step)) || (s = upload(c, csrc, &d.corner_src)) ||
@@ -886,6 +906,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_APPLY_PIPELINE:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
             c->apply_pipeline = (int)v;
+            return SEM_OK;
+        case SEM_OPT_RESIDENT:
+            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "resident inner solve must be 0 or 1");
+            c->resident = (int)v;
             return SEM_OK;
         case SEM_OPT_INNER_ITERATION:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "inner iteration must be 0 or 1");
@@ -1290,13 +1314,26 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
         SEM_CUDA(cudaGetLastError());
         mx.pinv32 = pinv;
     }
-    int grid = 0, kmax = 1;
+    int grid = 0, kmax = 1, rst = 0;
     size_t smem = 0;
-    dispatch_n(c->N, [&](auto nv) {
-        grid = solver_plan<decltype(nv)::value>(op, true, c->E, c->sms, kSolverSmemBudget, &kmax, &smem);
-        return cudaSuccess;
-    });
+    bool resident = false;
+    if (mx.fdm && c->resident)
+        dispatch_resident(c->N, [&](auto nv) {
+            resident = resident_plan<decltype(nv)::value>(c->E, c->sms, kResidentSmemBudget, &grid, &rst, &kmax,
+                                                          &smem);
+        });
+    if (!resident)
+        dispatch_n(c->N, [&](auto nv) {
+            grid = solver_plan<decltype(nv)::value>(op, true, c->E, c->sms, kSolverSmemBudget, &kmax, &smem);
+            return cudaSuccess;
+        });
     if (grid <= 0) return fail(SEM_ERR_CUDA, "could not size the cooperative grid");
+    unsigned long long* slots = nullptr;
+    if (resident) {
+        const size_t words = 2 * (size_t)grid * RESIDENT_SLOT_STRIDE;
+        if ((s = wsget(c, "res_slots", words, &slots))) return s;
+        SEM_CUDA(cudaMemsetAsync(slots, 0, words * sizeof(unsigned long long), c->stream));
+    }
     SolveArgs a{};
     a.kmax = kmax;
     a.op = op;
@@ -1317,13 +1354,21 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     SEM_CUDA(cudaMemsetAsync(sync, 0, sizeof(GridSync), c->stream));
     SEM_CUDA(cudaMemsetAsync(out, 0, sizeof(SolveOut), c->stream));
     if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[0], c->stream));
-    cudaError_t e = dispatch_n(c->N, [&](auto nv) {
-        return launch_solver<decltype(nv)::value>(c->dm, a, &w, &mx, grid, smem, c->stream);
-    });
+    cudaError_t e = cudaSuccess;
+    if (resident)
+        dispatch_resident(c->N, [&](auto nv) {
+            e = launch_resident<decltype(nv)::value>(c->dm, a, w, mx, c->D32_host.data(), c->S32_host.data(), rst,
+                                                     slots, grid, smem, c->stream);
+        });
+    else
+        e = dispatch_n(c->N, [&](auto nv) {
+            return launch_solver<decltype(nv)::value>(c->dm, a, &w, &mx, grid, smem, c->stream);
+        });
     if (e != cudaSuccess) return fail(SEM_ERR_CUDA, std::string("cooperative launch: ") + cudaGetErrorString(e));
     if (c->profile) SEM_CUDA(cudaEventRecord(c->ev[1], c->stream));
     c->stats.kernel_launches++;
     c->stats.solver_launches++;
+    if (resident) c->stats.resident_launches++;
     if ((s = finish_solve(c, out, sync, res))) return s;
     *sweeps = c->h_out->sweeps;
     c->stats.solver_iterations_fp32 += res->n_iter;
