@@ -82,6 +82,12 @@ enum sem_option {
     SEM_OPT_ADAPTIVE_INNER = 12, /* mixed mode: 1 (default) a sweep's inner tolerance is relaxed
                                     to what the outer test still needs (x 0.3), 0 always
                                     SEM_OPT_INNER_TOL */
+    SEM_OPT_PROJECT = 14,        /* mixed mode with SEM_GUESS_EXTRAPOLATE / _LEARNED, SDIRK
+                                    drivers: K in 1..24 replaces the extrapolation by the
+                                    projection onto the last K stage solutions (the guess
+                                    sum c_j z_j minimising |b - sum c_j b_j|, P. F. Fischer's
+                                    method for successive right-hand sides; the learned
+                                    correction then starts from it); 0 (default) off */
     SEM_OPT_RESIDENT = 13,       /* mixed mode, Res with SEM_PRECOND_FDM: 1 (default) keep the
                                     FP32 inner solve's vectors on chip (shared memory and
                                     registers; only element-ring copies are exchanged through
@@ -148,6 +154,9 @@ typedef struct {
     double learned_ratio_sum;       /* sum of |r(guess used)| / |r(extrapolated)| over learned guesses */
     long long resident_launches;    /* persistent solver launches with the on-chip inner solve
                                        (SEM_OPT_RESIDENT) */
+    long long projected_guesses;    /* stage guesses from the projection (SEM_OPT_PROJECT) */
+    double last_projection_ratio;   /* |b - sum c_j b_j| / |b| of the last one */
+    double projection_ratio_sum;    /* sum of that ratio over all projected guesses */
 } sem_stats;
 
 /* after each accepted step; nonzero return stops the time loop

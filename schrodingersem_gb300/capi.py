@@ -40,7 +40,8 @@ class SemStats(C.Structure):
                 ("solver_iterations_fp32", C.c_longlong), ("learned_guesses", C.c_longlong),
                 ("learned_accepted", C.c_longlong), ("last_guess_residual_ratio", C.c_double),
                 ("last_guess_theta", C.c_double), ("learned_ratio_sum", C.c_double),
-                ("resident_launches", C.c_longlong)]
+                ("resident_launches", C.c_longlong), ("projected_guesses", C.c_longlong),
+                ("last_projection_ratio", C.c_double), ("projection_ratio_sum", C.c_double)]
 
 
 class SemBatchStats(C.Structure):
@@ -130,6 +131,7 @@ OPT_SOLVE_PRECISION, OPT_INNER_TOL, OPT_STAGE_GUESS, OPT_WAIT_TIMEOUT_MS, OPT_MA
 OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_EXTRAP_ORDER = 7, 8, 9, 10, 11
 OPT_ADAPTIVE_INNER = 12
 OPT_RESIDENT = 13
+OPT_PROJECT = 14
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

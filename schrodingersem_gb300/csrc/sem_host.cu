@@ -88,6 +88,62 @@ __global__ void k_to_f32(long long n, const double* __restrict__ a, float* __res
         b[i] = (float)a[i];
 }
 
+// Projection stage guess (no counterpart in the reference): the previous
+// stage solutions z_j of the same operator and their right-hand sides b_j.
+constexpr int PROJ_MAX = 24;
+struct PtrList {
+    int nz;
+    const double* z[PROJ_MAX];
+    double c[PROJ_MAX];
+};
+
+// per-block partial sums of b.b_j (j < L.nz) and b.b, laid out
+// part[blk * (PROJ_MAX + 1) + j] (b.b at j = PROJ_MAX); fixed order.  On
+// masked vectors the plain sum equals the reference's unique-DOF dot.
+__global__ void __launch_bounds__(256) k_multidot(long long n, const double* __restrict__ b, PtrList L,
+                                                  double* __restrict__ part)
+{
+    double acc[PROJ_MAX + 1];
+#pragma unroll
+    for (int l = 0; l <= PROJ_MAX; ++l) acc[l] = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        const double bv = b[i];
+        acc[PROJ_MAX] = fma(bv, bv, acc[PROJ_MAX]);
+#pragma unroll
+        for (int l = 0; l < PROJ_MAX; ++l)
+            if (l < L.nz) acc[l] = fma(bv, __ldg(L.z[l] + i), acc[l]);
+    }
+    __shared__ double red[8][PROJ_MAX + 1];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int l = 0; l <= PROJ_MAX; ++l) {
+        double v = acc[l];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[wid][l] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x <= PROJ_MAX) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        part[(size_t)blockIdx.x * (PROJ_MAX + 1) + threadIdx.x] = v;
+    }
+}
+
+// out = sum_l c_l z_l over up to PROJ_MAX vectors
+__global__ void k_lincomb_n(long long n, PtrList L, double* __restrict__ out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+        double acc = 0.0;
+#pragma unroll
+        for (int l = 0; l < PROJ_MAX; ++l)
+            if (l < L.nz) acc = fma(L.c[l], __ldg(L.z[l] + i), acc);
+        out[i] = acc;
+    }
+}
+
 static int grid_1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 16); }
 
 // dynamic shared memory a persistent solver block may use for staging
@@ -242,6 +298,10 @@ struct sem_ctx {
     int extrap_order = 1;
     int adaptive_inner = 1;
     int resident = 1;
+    // projection stage guess: basis size (0 off), slots in use, next slot,
+    // Gram matrix b_i.b_j of the stored right-hand sides (proj_k^2)
+    int proj_k = 0, proj_count = 0, proj_head = 0;
+    std::vector<double> proj_G;
     // stage-guess history of the SDIRK drivers (persists across calls)
     long long hist_steps = 0;
     int hist_stages = 0;
@@ -882,6 +942,7 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
                 return fail(SEM_ERR_ARG, "bad guess mode");
             c->guess = (int)v;
             c->hist_steps = 0;  // a new guess mode starts a new history
+            c->proj_count = c->proj_head = 0;
             return SEM_OK;
         case SEM_OPT_WAIT_TIMEOUT_MS:
             if (!(v > 0)) return fail(SEM_ERR_ARG, "timeout must be positive");
@@ -906,6 +967,13 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_APPLY_PIPELINE:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
             c->apply_pipeline = (int)v;
+            return SEM_OK;
+        case SEM_OPT_PROJECT:
+            if (!(v >= 0 && v <= PROJ_MAX) || v != (double)(int)v)
+                return fail(SEM_ERR_ARG, "projection basis size must be an integer in [0, 24]");
+            c->proj_k = (int)v;
+            c->proj_count = c->proj_head = 0;
+            c->proj_G.assign((size_t)c->proj_k * c->proj_k, 0.0);
             return SEM_OK;
         case SEM_OPT_RESIDENT:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "resident inner solve must be 0 or 1");
@@ -1328,11 +1396,15 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
             return cudaSuccess;
         });
     if (grid <= 0) return fail(SEM_ERR_CUDA, "could not size the cooperative grid");
-    unsigned long long* slots = nullptr;
+    unsigned long long *slots = nullptr, *xa = nullptr, *xb = nullptr;
     if (resident) {
         const size_t words = 2 * (size_t)grid * RESIDENT_SLOT_STRIDE;
-        if ((s = wsget(c, "res_slots", words, &slots))) return s;
+        if ((s = wsget(c, "res_slots", words, &slots)) || (s = wsget(c, "res_xa", 2 * (size_t)c->n, &xa)) ||
+            (s = wsget(c, "res_xb", 2 * (size_t)c->n, &xb)))
+            return s;
         SEM_CUDA(cudaMemsetAsync(slots, 0, words * sizeof(unsigned long long), c->stream));
+        SEM_CUDA(cudaMemsetAsync(xa, 0, 2 * (size_t)c->n * sizeof(unsigned long long), c->stream));
+        SEM_CUDA(cudaMemsetAsync(xb, 0, 2 * (size_t)c->n * sizeof(unsigned long long), c->stream));
     }
     SolveArgs a{};
     a.kmax = kmax;
@@ -1358,7 +1430,7 @@ static int run_mixed(sem_ctx* c, int op, const double* pot, double alpha, double
     if (resident)
         dispatch_resident(c->N, [&](auto nv) {
             e = launch_resident<decltype(nv)::value>(c->dm, a, w, mx, c->D32_host.data(), c->S32_host.data(), rst,
-                                                     slots, grid, smem, c->stream);
+                                                     slots, xa, xb, grid, smem, c->stream);
         });
     else
         e = dispatch_n(c->N, [&](auto nv) {
@@ -1893,6 +1965,113 @@ extern "C" int sem_ctx_dataset(sem_ctx* c, void** X, float** T, long long* rows,
     return SEM_OK;
 }
 
+// ------------------------------------------------ projection stage guess
+// P. F. Fischer, "Projection techniques for iterative solution of Ax = b with
+// successive right-hand sides", Comput. Methods Appl. Mech. Engrg. 163
+// (1998), in a residual-minimising form for the indefinite stage operator:
+// the driver keeps the last proj_k stage solutions z_j with their right-hand
+// sides b_j (A z_j = b_j to the solver tolerance: every stage of an SDIRK or
+// BDF2 run at fixed dt has the same operator), and a new stage starts from
+// x0 = sum_j c_j z_j with c minimising |b - sum_j c_j b_j| (normal equations
+// on the Gram matrix of the b_j, Jacobi scaled, directions whose eigenvalue
+// is below 1e-13 of the largest dropped).  Slot j of the workspace holds z_j
+// (two planes) then b_j (two planes).
+static int proj_slots(sem_ctx* c, double** slots)
+{
+    return wsget(c, "proj_slots", (size_t)c->proj_k * 4 * c->n, slots);
+}
+
+// d[j] = b.b_j for every stored slot, *bb = b.b (one pass over the vectors)
+static int proj_dots(sem_ctx* c, const double* b, const double* slots, std::vector<double>& d, double* bb)
+{
+    const long long v = 2 * c->n;
+    PtrList L{};
+    L.nz = c->proj_count;
+    for (int j = 0; j < L.nz; ++j) L.z[j] = slots + (size_t)j * 2 * v + v;
+    constexpr int blocks = 256;
+    double* part = nullptr;
+    int s = wsget(c, "proj_part", (size_t)blocks * (PROJ_MAX + 1), &part);
+    if (s) return s;
+    k_multidot<<<blocks, 256, 0, c->stream>>>(v, b, L, part);
+    c->stats.kernel_launches++;
+    SEM_CUDA(cudaGetLastError());
+    SEM_CUDA(cudaMemcpyAsync(c->h_part, part, sizeof(double) * blocks * (PROJ_MAX + 1), cudaMemcpyDeviceToHost,
+                             c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    d.assign(L.nz, 0.0);
+    double acc = 0.0;
+    for (int q = 0; q < blocks; ++q) {
+        const double* row = c->h_part + (size_t)q * (PROJ_MAX + 1);
+        for (int j = 0; j < L.nz; ++j) d[j] += row[j];
+        acc += row[PROJ_MAX];
+    }
+    *bb = acc;
+    return SEM_OK;
+}
+
+// x0 = sum_j c_j z_j from the stored slots; returns the estimated relative
+// residual |b - sum c_j b_j| / |b| in *ratio (1 when no basis direction is
+// kept, then x0 = 0)
+static int proj_guess(sem_ctx* c, const double* slots, const std::vector<double>& d, double bb, double* x0,
+                      double* ratio)
+{
+    const int k = c->proj_count;
+    const int K = c->proj_k;
+    std::vector<double> sc(k), A((size_t)k * k), Q, cf(k, 0.0);
+    for (int i = 0; i < k; ++i) {
+        const double g = c->proj_G[(size_t)i * K + i];
+        sc[i] = g > 0 ? 1.0 / std::sqrt(g) : 0.0;
+    }
+    for (int i = 0; i < k; ++i)
+        for (int j = 0; j < k; ++j) A[(size_t)i * k + j] = sc[i] * c->proj_G[(size_t)i * K + j] * sc[j];
+    sym_eig_jacobi(k, A, Q);
+    double lmax = 0.0;
+    for (int i = 0; i < k; ++i) lmax = std::max(lmax, A[(size_t)i * k + i]);
+    for (int m = 0; m < k; ++m) {
+        const double lam = A[(size_t)m * k + m];
+        if (!(lam > 1e-13 * lmax)) continue;
+        double qd = 0.0;
+        for (int i = 0; i < k; ++i) qd += Q[(size_t)i * k + m] * sc[i] * d[i];
+        for (int i = 0; i < k; ++i) cf[i] += Q[(size_t)i * k + m] * qd / lam;
+    }
+    double cd = 0.0;
+    for (int i = 0; i < k; ++i) {
+        cf[i] *= sc[i];
+        cd += cf[i] * d[i];
+    }
+    PtrList L{};
+    L.nz = k;
+    for (int j = 0; j < k; ++j) {
+        L.z[j] = slots + (size_t)j * 4 * c->n;
+        L.c[j] = cf[j];
+    }
+    k_lincomb_n<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, L, x0);
+    c->stats.kernel_launches++;
+    SEM_CUDA(cudaGetLastError());
+    *ratio = bb > 0 ? std::sqrt(std::max(0.0, bb - cd) / bb) : 1.0;
+    return SEM_OK;
+}
+
+// store the solved stage (z, b) in the next slot and its Gram row (d, bb
+// from proj_dots with the same b)
+static int proj_push(sem_ctx* c, double* slots, const double* z, const double* b, const std::vector<double>& d,
+                     double bb)
+{
+    const int K = c->proj_k;
+    const int h = c->proj_head;
+    double* slot = slots + (size_t)h * 4 * c->n;
+    SEM_CUDA(cudaMemcpyAsync(slot, z, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    SEM_CUDA(cudaMemcpyAsync(slot + 2 * c->n, b, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    for (int j = 0; j < c->proj_count; ++j) {
+        if (j == h) continue;
+        c->proj_G[(size_t)h * K + j] = c->proj_G[(size_t)j * K + h] = d[j];
+    }
+    c->proj_G[(size_t)h * K + h] = bb;
+    c->proj_head = (h + 1) % K;
+    c->proj_count = std::min(c->proj_count + 1, K);
+    return SEM_OK;
+}
+
 static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, const double* V,
                        double T, const sem_solver_opts* o, sem_step_callback cb, void* user,
                        int* success)
@@ -1943,8 +2122,13 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             return s;
     }
     if (!extrap || c->hist_stages != stages || c->hist_dt != o->dt || sig[0] != c->hist_sig[0] ||
-        sig[1] != c->hist_sig[1])
+        sig[1] != c->hist_sig[1]) {
         c->hist_steps = 0;
+        c->proj_count = c->proj_head = 0;
+    }
+    const bool proj = extrap && c->proj_k > 0;
+    double* pslots = nullptr;
+    if (proj && (s = proj_slots(c, &pslots))) return s;
     c->hist_stages = stages;
     c->hist_dt = o->dt;
     const long long hist0 = c->hist_steps;
@@ -1977,13 +2161,25 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             if ((s = schro_rhs(&r, o->dt, zl, b))) return s;
             double* z = Z + (size_t)st * 2 * c->n;
             // initial guess: zero as the reference (schrodinger.hpp:222,379), or
-            // the stage's solution extrapolated from the previous steps: linear
-            // 2 z1 - z2, or (SEM_OPT_EXTRAP_ORDER 2) quadratic 3 z1 - 3 z2 + z3
+            // the projection onto the stored stage solutions (SEM_OPT_PROJECT),
+            // or the stage's solution extrapolated from the previous steps:
+            // linear 2 z1 - z2, or (SEM_OPT_EXTRAP_ORDER 2) quadratic
+            // 3 z1 - 3 z2 + z3
             int x_zero = 1;
             auto hz = [&](long long back) {
                 return Zring + (size_t)((gstep - back) % RING) * zset + (size_t)st * 2 * c->n;
             };
-            if (extrap && gstep >= 1) {
+            std::vector<double> pd;
+            double pbb = 0.0;
+            if (proj && (s = proj_dots(c, b, pslots, pd, &pbb))) return s;
+            if (proj && c->proj_count > 0) {
+                double ratio = 1.0;
+                if ((s = proj_guess(c, pslots, pd, pbb, z, &ratio))) return s;
+                c->stats.projected_guesses++;
+                c->stats.last_projection_ratio = ratio;
+                c->stats.projection_ratio_sum += ratio;
+                x_zero = 0;
+            } else if (extrap && gstep >= 1) {
                 const double* z1 = hz(1);
                 if (gstep >= 3 && c->extrap_order == 2) {
                     ZList q{};
@@ -2011,8 +2207,8 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             }
             // learned correction of the extrapolated guess, and/or a training
             // sample (the guess's residual features; its error after the solve)
-            const bool rec = extrap && gstep >= 2 && c->ds_cap > 0;
-            const bool use = extrap && gstep >= 2 && c->guess == SEM_GUESS_LEARNED && c->learner;
+            const bool rec = extrap && gstep >= 2 && !x_zero && c->ds_cap > 0;
+            const bool use = extrap && gstep >= 2 && !x_zero && c->guess == SEM_GUESS_LEARNED && c->learner;
             double* zext = nullptr;
             if (rec || use) {
                 if ((s = learned_guess(c, r.V, alpha, b, z, use, &zext))) return s;
@@ -2029,9 +2225,11 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
                 ok = false;
                 break;
             }
+            if (proj && (s = proj_push(c, pslots, z, b, pd, pbb))) return s;
         }
         if (!ok) {
             c->hist_steps = 0;
+            c->proj_count = c->proj_head = 0;
             break;
         }
         ZList zb{};

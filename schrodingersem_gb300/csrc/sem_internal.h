@@ -243,15 +243,16 @@ cudaError_t launch_solver(const DevMesh& m, const SolveArgs& a, const void* work
 // N = 5, 7, 9, 11.  resident_plan returns false when a block's share of the
 // mesh does not fit on chip; then the staged kernel (launch_solver) is used.
 // D32h / S32h: host FP32 copies of D and of the preconditioner basis S, both
-// row-major.  slots: 2 * grid * RESIDENT_SLOT_STRIDE words, cleared before
-// the launch.
+// row-major.  slots: 2 * grid * RESIDENT_SLOT_STRIDE words; xa, xb: 2 n words
+// each (the tagged ring exchange); all cleared before the launch.
 constexpr int RESIDENT_SLOT_STRIDE = 16;  // one 128-byte line per block's all-reduce word
 template <int N>
 bool resident_plan(int E, int sms, size_t smem_budget, int* grid, int* st, int* kmax64, size_t* smem);
 template <int N>
 cudaError_t launch_resident(const DevMesh& m, const SolveArgs& a, const KrylovWork<float>& w, const MixedArgs& mx,
-                            const float* D32h, const float* S32h, int st, unsigned long long* slots, int grid,
-                            size_t smem, cudaStream_t stream);
+                            const float* D32h, const float* S32h, int st, unsigned long long* slots,
+                            unsigned long long* xa, unsigned long long* xb, int grid, size_t smem,
+                            cudaStream_t stream);
 
 }  // namespace semgb
 

@@ -8,21 +8,22 @@
 // r_{i-1}, r_i, z_i, the element operator output and the preconditioner's
 // staging in shared memory, and the solution correction, the two direction
 // vectors and z_{i-1} in registers of the thread that owns the node.  Only the
-// element-ring copies (sides and corners, 4(N-1) of N^2 nodes) are written to
-// global memory, where the assembly gathers every copy of a shared node in the
-// library's fixed order (dss_value), so every copy of a node holds the same
+// element-ring copies (sides and corners, 4(N-1) of N^2 nodes) leave the SM:
+// each is published as a 64-bit word (FP32 value, epoch tag) and the
+// neighbours assemble every shared node from those words in the library's
+// fixed order (dss_value's sums), so every copy of a node holds the same
 // bits.  Per iteration:
 //   Phase B: y = DSS(A_local z_i)/beta_i - (beta_i/beta_{i-1}) r_{i-1};
 //            alpha partial z_i.y / beta_i; element preconditioner solves of y
-//            (ring copies to global)                           -> all-reduce
+//            (ring words out)                        -> exchange (alpha)
 //   Phase A: z_{i+1} = DSS(local solves) - (alpha_i/beta_i) z_i;
 //            y5 = y - (alpha_i/beta_i) r_i; beta_{i+1}^2 partial y5.z_{i+1};
-//            element operator of z_{i+1} (ring copies to global) -> all-reduce
+//            element operator of z_{i+1} (ring words out) -> exchange (beta)
 //   Givens rotation and the x / w update, in registers
 // which is the iteration of minres_core<N, float, OP_RES, 2> (Paige-Saunders
-// MINRES, include/minres.hpp:19-107 with a preconditioner).  The two
-// all-reduces are also the exchange barriers of the ring copies.
-//
+// MINRES, include/minres.hpp:19-107 with a preconditioner).  An exchange is
+// a grid all-reduce and the ring assembly at once (res_exchange).
+
 // Differences from the staged kernel, all at the FP32 inner solve's rounding
 // level: the right-hand side is scaled to unit norm (the correction is scaled
 // back into the FP64 solution), the scalar recurrences run in FP32 on every
@@ -36,12 +37,11 @@
 // so a pass reads and writes each value once in shared memory.
 //
 // All-reduce: each block publishes its partial as one 64-bit word (FP32
-// value, 32-bit epoch tag, each word on its own 128-byte line) after a
-// fence; every block's first warp polls the
-// grid's words (bounded by SEM_OPT_WAIT_TIMEOUT_MS through %globaltimer) and
-// sums them in one fixed order, so every block obtains the same bits.  Two
-// word sets alternate by epoch parity; the host clears them before each
-// launch.
+// value, 32-bit epoch tag, each word on its own 128-byte line); every block's
+// first warp polls the grid's words (bounded by SEM_OPT_WAIT_TIMEOUT_MS
+// through %globaltimer) and sums them in one fixed order, so every block
+// obtains the same bits.  Two word sets alternate by epoch parity; the host
+// clears them, and the ring words, before each launch.
 #pragma once
 #include "sem_solvers.cuh"
 
@@ -63,6 +63,8 @@ struct ResCoef {
 
 struct ResArgs {
     int st;                     // shared-memory plane length (max elements per block * N^2)
+    unsigned long long* xa;     // [2 n] tagged ring words of the operator output, zero at launch
+    unsigned long long* xb;     // [2 n] tagged ring words of the preconditioner output, zero at launch
     unsigned long long* slots;  // [2][gridDim.x][RES_WSTRIDE] tagged partial sums, zero at launch
 };
 
@@ -77,82 +79,11 @@ __device__ __forceinline__ unsigned long long res_ld(const unsigned long long* p
     return *(const volatile unsigned long long*)p;
 }
 
-// Grid all-reduce of one FP32 per-thread partial.  Every thread of every
-// block calls it; returns false (after recording gs->err) when a wait hit
-// its limit or another block reported one.  The block sum is formed in FP64
-// from per-warp FP32 sums; the published block partial is FP32.
-__device__ __forceinline__ bool res_allreduce(float v, unsigned long long* slots, unsigned& epoch, GridSync* gs,
-                                              long long tmo, double* red, double& out)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) red[wid] = (double)v;
-    ++epoch;
-    __syncthreads();
-    if (wid == 0) {
-        constexpr int nw = RES_TPB / 32;
-        double s = lane < nw ? red[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        const int G = gridDim.x;
-        unsigned long long* sl = slots + (size_t)(epoch & 1u) * G * RES_WSTRIDE;
-        if (lane == 0) {
-            __threadfence();  // ring copies and all earlier stores of the block before the word
-            *(volatile unsigned long long*)(sl + blockIdx.x * RES_WSTRIDE) = res_word((float)s, epoch);
-        }
-        unsigned long long u[RES_MAXQ];
-#pragma unroll
-        for (int k = 0; k < RES_MAXQ; ++k) {
-            const int q = lane + 32 * k;
-            u[k] = q < G ? res_ld(sl + q * RES_WSTRIDE) : res_word(0.f, epoch);
-        }
-        bool ok = true;
-        const unsigned long long t0 = global_ns();
-        unsigned polls = 0;
-        for (;;) {
-            bool ready = true;
-#pragma unroll
-            for (int k = 0; k < RES_MAXQ; ++k) ready &= (unsigned)(u[k] >> 32) == epoch;
-            if (ready) break;
-            if ((++polls & 31u) == 0) {
-                if (*(volatile int*)&gs->err) {
-                    ok = false;
-                    break;
-                }
-                if ((long long)(global_ns() - t0) > tmo) {
-                    atomicExch(&gs->err, 1);
-                    ok = false;
-                    break;
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < RES_MAXQ; ++k) {
-                const int q = lane + 32 * k;
-                if (q < G && (unsigned)(u[k] >> 32) != epoch) u[k] = res_ld(sl + q * RES_WSTRIDE);
-            }
-        }
-        double acc = 0.0;
-#pragma unroll
-        for (int k = 0; k < RES_MAXQ; ++k) acc += (double)__uint_as_float((unsigned)u[k]);
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        ok = __all_sync(0xffffffffu, ok);
-        __threadfence();  // the other blocks' ring copies are read after this
-        if (lane == 0) {
-            red[32] = acc;
-            red[33] = ok ? 1.0 : 0.0;
-        }
-    }
-    __syncthreads();
-    out = red[32];
-    return red[33] != 0.0;
-}
-
 // ---------------------------------------------------------------- line passes
 // xi lines (c, le, j): N consecutive values from base = c*st + le*N^2 + j*N;
-// eta lines (c, le, i): stride N from base = c*st + le*N^2 + i.  Lines of one
-// pass are disjoint, so each pass may write in place.
+// eta lines (c, le, i): stride N from base = c*st + le*N^2 + i.  Line L is
+// (c, pos, le) with the element fastest.  Lines of one pass are disjoint, so
+// each pass may write in place.
 template <int N>
 __device__ __forceinline__ void res_line(int L, int ne, int st, bool xi, int& base, int& fb, int& pos)
 {
@@ -160,8 +91,10 @@ __device__ __forceinline__ void res_line(int L, int ne, int st, bool xi, int& ba
     const int per = ne * N;
     const int c = L >= per ? 1 : 0;
     const int rem = L - c * per;
-    const int le = rem / N;
-    pos = rem - le * N;
+    pos = rem / ne;  // j of a xi line, i of an eta line
+    // consecutive threads take the same line of consecutive elements: with an
+    // odd N the element stride N^2 spreads a warp over all 32 banks
+    const int le = rem - pos * ne;
     fb = le * NN + (xi ? pos * N : pos);
     base = c * st + fb;
 }
@@ -258,7 +191,8 @@ __device__ __forceinline__ void res_apply_y2(const ResCoef<N>& cf, float* A, con
 
 // preconditioner passes on B in place (fdm_range_post's four contractions):
 // F1 t = S^T u along xi; F2 u = d * (t S) along eta; F3 t = S u along xi;
-// F4 z = t S^T along eta, times the Neumann-Neumann weight, ring copies to Gout
+// F4 z = t S^T along eta, times the Neumann-Neumann weight, ring copies to Xout
+// (tagged words, see res_exchange)
 template <int N>
 __device__ __forceinline__ void res_fdm_xi(const ResCoef<N>& cf, float* B, int ne, int st, bool transpose)
 {
@@ -298,8 +232,8 @@ __device__ __forceinline__ void res_fdm_f2(const ResCoef<N>& cf, float* B, const
 }
 
 template <int N>
-__device__ __forceinline__ void res_fdm_f4(const ResCoef<N>& cf, float* B, const float* WT, float* Gout, int ne,
-                                           int st, long long n, int eb)
+__device__ __forceinline__ void res_fdm_f4(const ResCoef<N>& cf, float* B, const float* WT, unsigned long long* Xout,
+                                           unsigned tag, int ne, int st, long long n, int eb)
 {
     constexpr int NN = N * N;
     for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
@@ -319,7 +253,7 @@ __device__ __forceinline__ void res_fdm_f4(const ResCoef<N>& cf, float* B, const
             for (int b = 0; b < N; ++b) acc = fmaf(t[b], cf.S[j * N + b], acc);
             const float z = WT[fb + j * N] * acc;
             B[base + j * N] = z;
-            if (side_i || j == 0 || j == N - 1) Gout[gbase + (long long)j * N] = z;
+            if (side_i || j == 0 || j == N - 1) __stcg(Xout + gbase + (long long)j * N, res_word(z, tag));
         }
     }
 }
@@ -360,22 +294,28 @@ __device__ __forceinline__ void res_setup(const DevMesh& m, float* sm, int st, i
 }
 
 // Assembly of the ring copies in place (continuous format, dss_value's
-// sums): the element-local planes P (two components) hold this block's
-// partials, G the partials of every block (the ring copies were published
-// before the last all-reduce).  One task per element side and component
-// (its N-2 side nodes: own + the neighbour's copy, whose flat indices are
-// side_base + k side_step) and one per element corner and component (the
-// corner node's copies in CSR order), so all loads of a task are independent
-// and the whole gather costs one round trip to L2.  Dirichlet boundary
-// copies become zero; lone (Neumann) sides keep their own value.
+// sums), from tagged words.  The element-local planes P (two components) hold
+// this block's partials; X holds every block's ring partials as 64-bit words
+// (FP32 value, epoch tag `tag`), so a load that returns the right tag is the
+// data itself: no flag, fence or barrier stands between a neighbour's store
+// and its use.  One task per element side and component (its N-2 side
+// nodes: own + the neighbour's copy at side_base + k side_step) and one per
+// element corner and component (the corner node's copies in CSR order);
+// stale words are reloaded until their tag matches (bounded: returns false
+// after recording gs->err when tmo runs out).  Dirichlet boundary copies
+// become zero; lone (Neumann) sides keep their own value.  Threads
+// [t_first, RES_TPB) take the tasks.
 template <int N>
-__device__ __forceinline__ void res_ring(const DevMesh& m, const float* G, float* P, int st, int eb, int ne)
+__device__ __forceinline__ bool res_ring(const DevMesh& m, const unsigned long long* X, float* P, int st, int eb,
+                                         int ne, unsigned tag, int t_first, GridSync* gs, long long tmo)
 {
     constexpr int NN = N * N;
     const long long n = m.n;
     const int nside = ne * 8;  // (element, side, component)
     const int ntask = ne * 16;
-    for (int t = threadIdx.x; t < ntask; t += RES_TPB) {
+    bool ok = true;
+    const unsigned long long t0 = global_ns();
+    for (int t = threadIdx.x - t_first; t < ntask && ok; t += RES_TPB - t_first) {
         const bool corner = t >= nside;
         const int u = corner ? t - nside : t;
         const int c = u & 1;
@@ -384,55 +324,166 @@ __device__ __forceinline__ void res_ring(const DevMesh& m, const float* G, float
         const int e = eb + le;
         const int fl = __ldg(m.flags + e);
         float* pe = P + c * st + le * NN;
-        const float* g = G + (long long)c * n;
+        const unsigned long long* x = X + (long long)c * n;
         if (!corner) {
-            const int sb = __ldg(m.side_base + 4 * e + sc), ss = __ldg(m.side_step + 4 * e + sc);
-            // side node k (1..N-2) of side sc: local index
             const int l0 = sc == 0 ? 0 : sc == 1 ? N - 1 : sc == 2 ? (N - 1) * N : 0;
             const int lk = (sc == 0 || sc == 2) ? 1 : N;
             if ((fl >> (4 + sc)) & 1) {  // Dirichlet boundary side
 #pragma unroll
                 for (int k = 1; k < N - 1; ++k) pe[l0 + k * lk] = 0.f;
             } else if (!((fl >> (16 + sc)) & 1)) {  // interior side: own + other
-                float v[N];
+                const long long sb = __ldg(m.side_base + 4 * e + sc), ss = __ldg(m.side_step + 4 * e + sc);
+                unsigned long long w[N];
 #pragma unroll
-                for (int k = 1; k < N - 1; ++k) v[k] = __ldcg(g + (long long)sb + (long long)k * ss);
+                for (int k = 1; k < N - 1; ++k) w[k] = res_ld(x + sb + k * ss);
+                for (unsigned polls = 1;; ++polls) {
+                    bool ready = true;
 #pragma unroll
-                for (int k = 1; k < N - 1; ++k) pe[l0 + k * lk] = pe[l0 + k * lk] + v[k];
+                    for (int k = 1; k < N - 1; ++k) ready &= (unsigned)(w[k] >> 32) == tag;
+                    if (ready) break;
+                    if ((polls & 31u) == 0 &&
+                        (*(volatile int*)&gs->err || (long long)(global_ns() - t0) > tmo)) {
+                        atomicExch(&gs->err, 1);
+                        ok = false;
+                        break;
+                    }
+#pragma unroll
+                    for (int k = 1; k < N - 1; ++k)
+                        if ((unsigned)(w[k] >> 32) != tag) w[k] = res_ld(x + sb + k * ss);
+                }
+#pragma unroll
+                for (int k = 1; k < N - 1; ++k)
+                    pe[l0 + k * lk] = pe[l0 + k * lk] + __uint_as_float((unsigned)w[k]);
             }
         } else {
             const int lc = sc == 0 ? 0 : sc == 1 ? N - 1 : sc == 2 ? NN - 1 : (N - 1) * N;
             if ((fl >> (12 + sc)) & 1) {  // Dirichlet boundary corner
                 pe[lc] = 0.f;
+                continue;
+            }
+            const int* cl = m.corner_nb + (size_t)(4 * e + sc) * CORNER_NB_MAX;
+            int q[CORNER_NB_MAX];
+#pragma unroll
+            for (int k = 0; k < CORNER_NB_MAX; ++k) q[k] = __ldg(cl + k);
+            float sum = 0.f;  // csum = 0, then += in connected_elements order
+            if (q[0] == -2) {  // more copies than the table holds: the CSR, one by one
+                const int node = __ldg(m.corner_node + 4 * e + sc);
+                const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
+                for (int k = q0; k < q1 && ok; ++k) {
+                    const int f = __ldg(m.node_flat + k);
+                    unsigned long long v = res_ld(x + f);
+                    for (unsigned polls = 1; (unsigned)(v >> 32) != tag; ++polls) {
+                        if ((polls & 31u) == 0 &&
+                            (*(volatile int*)&gs->err || (long long)(global_ns() - t0) > tmo)) {
+                            atomicExch(&gs->err, 1);
+                            ok = false;
+                            break;
+                        }
+                        v = res_ld(x + f);
+                    }
+                    sum += __uint_as_float((unsigned)v);
+                }
             } else {
-                const int* cl = m.corner_nb + (size_t)(4 * e + sc) * CORNER_NB_MAX;
-                int q[CORNER_NB_MAX];
+                unsigned long long w[CORNER_NB_MAX];
 #pragma unroll
-                for (int k = 0; k < CORNER_NB_MAX; ++k) q[k] = __ldg(cl + k);
-                float sum = 0.f;  // csum = 0, then += in connected_elements order
-                if (q[0] == -2) {  // more copies than the table holds: the CSR
-                    const int node = __ldg(m.corner_node + 4 * e + sc);
-                    const int q0 = __ldg(m.node_ptr + node), q1 = __ldg(m.node_ptr + node + 1);
-                    for (int k = q0; k < q1; ++k) sum += __ldcg(g + __ldg(m.node_flat + k));
-                } else {
-                    float v[CORNER_NB_MAX];
+                for (int k = 0; k < CORNER_NB_MAX; ++k) w[k] = q[k] >= 0 ? res_ld(x + q[k]) : res_word(0.f, tag);
+                for (unsigned polls = 1;; ++polls) {
+                    bool ready = true;
 #pragma unroll
-                    for (int k = 0; k < CORNER_NB_MAX; ++k) v[k] = q[k] >= 0 ? __ldcg(g + q[k]) : 0.f;
+                    for (int k = 0; k < CORNER_NB_MAX; ++k) ready &= (unsigned)(w[k] >> 32) == tag;
+                    if (ready) break;
+                    if ((polls & 31u) == 0 &&
+                        (*(volatile int*)&gs->err || (long long)(global_ns() - t0) > tmo)) {
+                        atomicExch(&gs->err, 1);
+                        ok = false;
+                        break;
+                    }
 #pragma unroll
                     for (int k = 0; k < CORNER_NB_MAX; ++k)
-                        if (q[k] >= 0) sum += v[k];
+                        if ((unsigned)(w[k] >> 32) != tag) w[k] = res_ld(x + q[k]);
                 }
-                pe[lc] = sum;
+#pragma unroll
+                for (int k = 0; k < CORNER_NB_MAX; ++k)
+                    if (q[k] >= 0) sum += __uint_as_float((unsigned)w[k]);
             }
+            pe[lc] = sum;
         }
     }
+    return ok;
+}
+
+// One phase boundary: the grid all-reduce of v (first warp: publish this
+// block's word, poll every block's) and, at the same time, the in-place ring
+// assembly of P from the tagged words X (the other warps).  Both wait for the
+// same stores of the other blocks, so the phase costs one round trip after
+// the last of them.  The ring words and the all-reduce word carry the same
+// epoch.  Returns false when a wait hit its limit.
+template <int N>
+__device__ __forceinline__ bool res_exchange(float v, const DevMesh& m, const unsigned long long* X, float* P, int st,
+                                             int eb, int ne, unsigned long long* slots, unsigned& epoch,
+                                             GridSync* gs, long long tmo, double* red, double& out)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid] = (double)v;
+    ++epoch;
+    __syncthreads();
+    bool ok = true;
+    if (wid == 0) {
+        constexpr int nw = RES_TPB / 32;
+        double s = lane < nw ? red[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        const int G = gridDim.x;
+        unsigned long long* sl = slots + (size_t)(epoch & 1u) * G * RES_WSTRIDE;
+        if (lane == 0) *(volatile unsigned long long*)(sl + blockIdx.x * RES_WSTRIDE) = res_word((float)s, epoch);
+        unsigned long long u[RES_MAXQ];
+#pragma unroll
+        for (int k = 0; k < RES_MAXQ; ++k) {
+            const int q = lane + 32 * k;
+            u[k] = q < G ? res_ld(sl + q * RES_WSTRIDE) : res_word(0.f, epoch);
+        }
+        const unsigned long long t0 = global_ns();
+        for (unsigned polls = 1;; ++polls) {
+            bool ready = true;
+#pragma unroll
+            for (int k = 0; k < RES_MAXQ; ++k) ready &= (unsigned)(u[k] >> 32) == epoch;
+            if (ready) break;
+            if ((polls & 31u) == 0) {
+                if (*(volatile int*)&gs->err || (long long)(global_ns() - t0) > tmo) {
+                    atomicExch(&gs->err, 1);
+                    ok = false;
+                    break;
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < RES_MAXQ; ++k) {
+                const int q = lane + 32 * k;
+                if (q < G && (unsigned)(u[k] >> 32) != epoch) u[k] = res_ld(sl + q * RES_WSTRIDE);
+            }
+        }
+        double acc = 0.0;
+#pragma unroll
+        for (int k = 0; k < RES_MAXQ; ++k) acc += (double)__uint_as_float((unsigned)u[k]);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) red[32] = acc;
+    } else {
+        ok = res_ring<N>(m, X, P, st, eb, ne, epoch, 32, gs, tmo);
+    }
+    const bool fail = __syncthreads_or(!ok) != 0;
+    out = red[32];
+    return !fail;
 }
 
 // Res combination on the line passes' laplacian (planes A), ring copies of
-// the element-local result to the global exchange field G
+// the element-local result to the exchange words X (tag: the epoch of the
+// exchange that reads them)
 template <int N>
-__device__ __forceinline__ void res_combine(const float* U, float* A, const float* MS, const float* MV, float* G,
-                                            int st, int eb, int nl, float alpha, long long n)
+__device__ __forceinline__ void res_combine(const float* U, float* A, const float* MS, const float* MV,
+                                            unsigned long long* X, unsigned tag, int st, int eb, int nl, float alpha,
+                                            long long n)
 {
     constexpr int NN = N * N;
 #pragma unroll
@@ -449,8 +500,8 @@ __device__ __forceinline__ void res_combine(const float* U, float* A, const floa
             A[st + l] = o1;
             if ((i == 0) | (i == N - 1) | (j == 0) | (j == N - 1)) {
                 const long long flat = (long long)(eb + le) * NN + node;
-                G[flat] = o0;
-                G[n + flat] = o1;
+                __stcg(X + flat, res_word(o0, tag));
+                __stcg(X + n + flat, res_word(o1, tag));
             }
         }
     }
@@ -458,7 +509,7 @@ __device__ __forceinline__ void res_combine(const float* U, float* A, const floa
 
 template <int N>
 __device__ __forceinline__ void res_apply(const ResCoef<N>& cf, float* sm, int st, int eb, int ne, float alpha,
-                                          float* GY, long long n)
+                                          unsigned long long* X, unsigned tag, long long n)
 {
     float* U = sm + 8 * st;
     float* A = sm + 10 * st;
@@ -472,12 +523,12 @@ __device__ __forceinline__ void res_apply(const ResCoef<N>& cf, float* sm, int s
     __syncthreads();
     res_apply_y2<N>(cf, A, B, ne, st);
     __syncthreads();
-    res_combine<N>(U, A, sm + 3 * st, sm + 4 * st, GY, st, eb, ne * N * N, alpha, n);
+    res_combine<N>(U, A, sm + 3 * st, sm + 4 * st, X, tag, st, eb, ne * N * N, alpha, n);
 }
 
 template <int N>
-__device__ __forceinline__ void res_precond(const ResCoef<N>& cf, float* sm, int st, int eb, int ne, float* GY3,
-                                            long long n)
+__device__ __forceinline__ void res_precond(const ResCoef<N>& cf, float* sm, int st, int eb, int ne,
+                                            unsigned long long* X, unsigned tag, long long n)
 {
     float* B = sm + 12 * st;
     __syncthreads();
@@ -487,7 +538,7 @@ __device__ __forceinline__ void res_precond(const ResCoef<N>& cf, float* sm, int
     __syncthreads();
     res_fdm_xi<N>(cf, B, ne, st, false);
     __syncthreads();
-    res_fdm_f4<N>(cf, B, sm + 6 * st, GY3, ne, st, n, eb);
+    res_fdm_f4<N>(cf, B, sm + 6 * st, X, tag, ne, st, n, eb);
 }
 
 struct ResOut {
@@ -501,8 +552,9 @@ struct ResOut {
 // when a wait hit its limit.
 template <int N>
 __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf, float* sm, int st, int eb, int ne,
-                                          const double* const* r64, double rn, float alpha, float* GY, float* GY3,
-                                          unsigned long long* slots, unsigned& epoch, GridSync* gs, long long tmo,
+                                          const double* const* r64, double rn, float alpha, unsigned long long* XA,
+                                          unsigned long long* XB, unsigned long long* slots, unsigned& epoch,
+                                          GridSync* gs, long long tmo,
                                           double* red, int maxit, float tol_rel, double* const* xp, ResOut& res)
 {
     constexpr int NN = N * N;
@@ -542,12 +594,10 @@ __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf
             }
         }
     }
-    res_precond<N>(cf, sm, st, eb, ne, GY3, n);
+    res_precond<N>(cf, sm, st, eb, ne, XB, epoch + 1, n);
     double dummy = 0.0;
-    if (!res_allreduce(0.f, slots, epoch, gs, tmo, red, dummy)) return false;
-    // ---- P1: z_1 = DSS(local solves); |r|_P^2 = r.z; A = A_local(z_1)
-    res_ring<N>(m, GY3, B, st, eb, ne);
-    __syncthreads();
+    if (!res_exchange<N>(0.f, m, XB, B, st, eb, ne, slots, epoch, gs, tmo, red, dummy)) return false;
+    // ---- P1: z_1 = DSS(local solves) (assembled in B); |r|_P^2 = r.z; A = A_local(z_1)
     float pz = 0.f;
 #pragma unroll
     for (int k = 0; k < RES_NPT; ++k) {
@@ -560,9 +610,9 @@ __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf
             pz = fmaf(OW[l] * Rb[st + l], z1, pz);
         }
     }
-    res_apply<N>(cf, sm, st, eb, ne, alpha, GY, n);
+    res_apply<N>(cf, sm, st, eb, ne, alpha, XA, epoch + 1, n);
     double bz = 0.0;
-    if (!res_allreduce(pz, slots, epoch, gs, tmo, red, bz)) return false;
+    if (!res_exchange<N>(pz, m, XA, A, st, eb, ne, slots, epoch, gs, tmo, red, bz)) return false;
     if (!(bz > 0.0)) {  // r . P^-1 r = 0: nothing to solve
         res.conv = true;
         return true;
@@ -575,9 +625,7 @@ __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf
     int it = 1;
     bool conv = false;
     for (;;) {
-        // ---- Phase B_it
-        res_ring<N>(m, GY, A, st, eb, ne);
-        __syncthreads();
+        // ---- Phase B_it (A holds the assembled A z_i)
         float s1 = 0.f;
 #pragma unroll
         for (int k = 0; k < RES_NPT; ++k) {
@@ -595,14 +643,12 @@ __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf
                 }
             }
         }
-        res_precond<N>(cf, sm, st, eb, ne, GY3, n);
+        res_precond<N>(cf, sm, st, eb, ne, XB, epoch + 1, n);
         double S1 = 0.0;
-        if (!res_allreduce(s1, slots, epoch, gs, tmo, red, S1)) return false;
+        if (!res_exchange<N>(s1, m, XB, B, st, eb, ne, slots, epoch, gs, tmo, red, S1)) return false;
         const float alpha_i = (float)S1;
         const float c2 = alpha_i * inv_beta;
-        // ---- Phase A_it+1
-        res_ring<N>(m, GY3, B, st, eb, ne);
-        __syncthreads();
+        // ---- Phase A_it+1 (B holds the assembled local solves)
         float ss = 0.f;
 #pragma unroll
         for (int k = 0; k < RES_NPT; ++k) {
@@ -622,9 +668,9 @@ __device__ __forceinline__ bool res_inner(const DevMesh& m, const ResCoef<N>& cf
                 }
             }
         }
-        res_apply<N>(cf, sm, st, eb, ne, alpha, GY, n);
+        res_apply<N>(cf, sm, st, eb, ne, alpha, XA, epoch + 1, n);
         double bnew2d = 0.0;
-        if (!res_allreduce(ss, slots, epoch, gs, tmo, red, bnew2d)) return false;
+        if (!res_exchange<N>(ss, m, XA, A, st, eb, ne, slots, epoch, gs, tmo, red, bnew2d)) return false;
         {
             float* tmp = Ra;  // r_{i-1} <- r_i, r_i <- y5
             Ra = Rb;
@@ -782,7 +828,7 @@ __global__ void __launch_bounds__(RES_TPB, 1)
         }
         const double* r64c[2] = {mx.r64[0], mx.r64[1]};
         ResOut ir{};
-        if (!res_inner<N>(m, cf, sm, st, eb, ne, r64c, sweep_state[1], alpha32, w.Y[0], w.Y3, ra.slots, epoch,
+        if (!res_inner<N>(m, cf, sm, st, eb, ne, r64c, sweep_state[1], alpha32, ra.xa, ra.xb, ra.slots, epoch,
                           a.sync, a.timeout_ns, red, budget, (float)itol, xp, ir))
             return;
         inner_total += ir.it;
@@ -835,8 +881,9 @@ bool resident_plan(int E, int sms, size_t smem_budget, int* grid_out, int* st_ou
 
 template <int N>
 cudaError_t launch_resident(const DevMesh& m, const SolveArgs& a, const KrylovWork<float>& w, const MixedArgs& mx,
-                            const float* D32h, const float* S32h, int st, unsigned long long* slots, int grid,
-                            size_t smem, cudaStream_t stream)
+                            const float* D32h, const float* S32h, int st, unsigned long long* slots,
+                            unsigned long long* xa, unsigned long long* xb, int grid, size_t smem,
+                            cudaStream_t stream)
 {
     const void* fn = (const void*)k_minres_resident<N>;
     // a per-device function attribute: set on every launch (cheap), so a
@@ -852,7 +899,7 @@ cudaError_t launch_resident(const DevMesh& m, const SolveArgs& a, const KrylovWo
         cf.D[q] = D32h[q];
         cf.S[q] = S32h[q];
     }
-    ResArgs ra{st, slots};
+    ResArgs ra{st, xa, xb, slots};
     void* args[] = {&mm, &aa, &ww, &xx, &cf, &ra};
     return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(RES_TPB), args, smem, stream);
 }
@@ -861,6 +908,7 @@ cudaError_t launch_resident(const DevMesh& m, const SolveArgs& a, const KrylovWo
     template bool resident_plan<NV>(int, int, size_t, int*, int*, int*, size_t*);                             \
     template cudaError_t launch_resident<NV>(const DevMesh&, const SolveArgs&, const KrylovWork<float>&,      \
                                              const MixedArgs&, const float*, const float*, int,               \
-                                             unsigned long long*, int, size_t, cudaStream_t);
+                                             unsigned long long*, unsigned long long*, unsigned long long*, int,   \
+                                             size_t, cudaStream_t);
 
 }  // namespace semgb
