@@ -82,6 +82,11 @@ enum sem_option {
     SEM_OPT_ADAPTIVE_INNER = 12, /* mixed mode: 1 (default) a sweep's inner tolerance is relaxed
                                     to what the outer test still needs (x 0.3), 0 always
                                     SEM_OPT_INNER_TOL */
+    SEM_OPT_LEARNED_STEP = 15,   /* SEM_GUESS_LEARNED: 0 (default) move from the base guess along
+                                    the predicted correction by the step that minimises the FP64
+                                    residual; 1 take the whole predicted correction (the MINRES
+                                    solve removes its high-frequency error quickly), unless its
+                                    residual is not finite or more than 10x the base's */
     SEM_OPT_PROJECT = 14,        /* mixed mode with SEM_GUESS_EXTRAPOLATE / _LEARNED, SDIRK
                                     drivers: K in 1..24 replaces the extrapolation by the
                                     projection onto the last K stage solutions (the guess

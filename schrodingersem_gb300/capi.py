@@ -132,6 +132,7 @@ OPT_PRECOND, OPT_INNER_ITERATION, OPT_REFINE_TOL_SCALE, OPT_APPLY_PIPELINE, OPT_
 OPT_ADAPTIVE_INNER = 12
 OPT_RESIDENT = 13
 OPT_PROJECT = 14
+OPT_LEARNED_STEP = 15
 PREC_FP64, PREC_MIXED = 0, 1
 PRECOND_NONE, PRECOND_DIAG, PRECOND_FDM = 0, 1, 2
 GUESS_ZERO, GUESS_EXTRAPOLATE, GUESS_LEARNED = 0, 1, 2

@@ -296,6 +296,7 @@ struct sem_ctx {
     double outer_scale = 1.0;
     int apply_pipeline = 1;
     int extrap_order = 1;
+    int learned_step = 0;  // SEM_OPT_LEARNED_STEP
     int adaptive_inner = 1;
     int resident = 1;
     // projection stage guess: basis size (0 off), slots in use, next slot,
@@ -967,6 +968,10 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
         case SEM_OPT_APPLY_PIPELINE:
             if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
             c->apply_pipeline = (int)v;
+            return SEM_OK;
+        case SEM_OPT_LEARNED_STEP:
+            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "learned step must be 0 or 1");
+            c->learned_step = (int)v;
             return SEM_OK;
         case SEM_OPT_PROJECT:
             if (!(v >= 0 && v <= PROJ_MAX) || v != (double)(int)v)
@@ -1875,7 +1880,10 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
         return s;
     const double rx = x1 + x2;
     const double den = n_ext - 2.0 * rx + n_l;
-    const double theta = den > 0 ? (n_ext - rx) / den : 0.0;
+    double theta = den > 0 ? (n_ext - rx) / den : 0.0;
+    // full step: the prediction as it is, unless it is not finite or raises
+    // the residual more than tenfold (then the residual-minimising step)
+    if (c->learned_step == 1 && std::isfinite(n_l) && n_l <= 100.0 * n_ext) theta = 1.0;
     c->stats.learned_guesses++;
     double ratio = 1.0;
     if (theta > 0 && n_ext > 0) {
@@ -1883,7 +1891,8 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
         c->stats.kernel_launches++;
         SEM_CUDA(cudaGetLastError());
         c->stats.learned_accepted++;
-        ratio = std::sqrt(std::max(0.0, n_ext - (n_ext - rx) * (n_ext - rx) / den) / n_ext);
+        const double n_t = n_ext - 2.0 * theta * (n_ext - rx) + theta * theta * den;  // |r_ext - theta A d|^2
+        ratio = std::sqrt(std::max(0.0, n_t) / n_ext);
     }
     c->stats.last_guess_residual_ratio = ratio;
     c->stats.last_guess_theta = theta;
