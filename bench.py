@@ -951,6 +951,96 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+# ================================================================= CPU baselines of the other configs
+def _timed(fn, reps=1):
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = fn()
+    return (time.perf_counter() - t0) / reps, out
+
+
+def run_cpu_legs(a):
+    """The reference's own OpenMP build (oracle/ref, all host threads) on the
+    configurations the headline line does not cover, each beside the same
+    quantity on the GPU: c1 (the whole Poisson solve: 16x16 quads on [0,1]^2
+    jittered 0.15h seed 0, p = 4, PCG 1e-12), the Res apply (64x64 quads,
+    p = 8, algorithmic bytes 9 words/node), and bounded MINRES samples of the
+    c4 (128x128, p = 8) and c5 (384x384, p = 12) stage solves: seconds per
+    reference MINRES iteration on the stage operator (capped sample), next
+    to the GPU's plain FP64 MINRES seconds per iteration on the same
+    operator.  One JSON line."""
+    import torch
+
+    import schrodingersem_gb300 as S
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.meshgen import structured_quads
+    S.build()
+    R, why = _reference_or_port()
+    if R is None:
+        print(json.dumps({"leg": "cpu", "unavailable": why}), flush=True)
+        return
+    threads = cpu_threads()
+    R.set_threads(threads)
+    out = {"threads": threads}
+    # ---- c1
+    co, el = structured_quads(16, box=(0.0, 1.0, 0.0, 1.0), jitter=0.15, seed=0)
+    rm = _ref_mesh(R, 4, co, el)
+    X, Y = rm.node_coords()
+    f = 2 * math.pi ** 2 * np.sin(math.pi * X) * np.sin(math.pi * Y)  # poisson() projects f itself
+    t_ref, (u_ref, (ok_r, it_r, _)) = _timed(lambda: rm.poisson(rm.zeros(), f, 10 * rm.dof(), 1e-12), 5)
+    ctx = S.Context(4, coords=co, elements=el)
+    f_d = np.ascontiguousarray(f)
+    for _ in range(3):
+        ctx.poisson(np.zeros(ctx.shape), f_d, 10 * ctx.dof(), 1e-12)
+    torch.cuda.synchronize()
+    t_gpu, (ok_g, it_g, _) = _timed(lambda: ctx.poisson(np.zeros(ctx.shape), f_d, 10 * ctx.dof(), 1e-12), 20)
+    out["c1"] = {"unit": "s per Poisson solve (PCG 1e-12, host arrays in and out)", "reference_cpu": t_ref,
+                 "reference_iterations": it_r, "gpu": t_gpu, "gpu_iterations": it_g, "speedup": t_ref / t_gpu}
+    ctx.close()
+    # ---- Res apply at the c2 mesh
+    co, el = workload_inputs()
+    rm = _ref_mesh(R, P, co, el)
+    X, Y = rm.node_coords()
+    qr, qi = np.cos(X) * np.exp(-Y * Y / 8), np.sin(X) * np.exp(-Y * Y / 8)
+    V = X * X + Y * Y
+    rm.schro_res(V, 0.01, qr, qi)
+    t_app, _ = _timed(lambda: rm.schro_res(V, 0.01, qr, qi), 5)
+    nloc = rm.zeros().size
+    out["apply"] = {"mesh": "64x64 quads, p = 8 (331,776 element-local nodes per component)",
+                    "reference_cpu_s": t_app, "reference_cpu_gbs_algorithmic": nloc * 8 * 9 / t_app / 1e9,
+                    "note": "FP64, 9 words/node; includes the reference's unmask/global_sum/mask"}
+    # ---- bounded MINRES samples of the c4 / c5 stage operators
+    for name, n, p, box, cap in (("c4", 128, 8, 10.0, 30), ("c5", 384, 12, 12.0, 4)):
+        co, el = structured_quads(n, box=(-box, box, -box, box), jitter=0.1, seed=1)
+        t0 = time.perf_counter()
+        rm = _ref_mesh(R, p, co, el)
+        setup = time.perf_counter() - t0
+        X, Y = rm.node_coords()
+        V = 0.5 * (X * X + Y * Y)
+        br, bi = rm.schro_f(V, np.exp(-X * X - Y * Y), np.zeros_like(X))
+        alpha = 0.25 * 2.5e-3
+        t_it, _ = _timed(lambda: rm.minres_res(V, alpha, br * 2.5e-3, bi * 2.5e-3, rm.zeros(), rm.zeros(), cap,
+                                               1e-30))
+        del rm
+        ctx = S.Context(p, coords=co, elements=el)
+        ctx.set_option(capi.OPT_PROFILE, 1)
+        dV = ctx.to_device(V)
+        dbr, dbi = ctx.to_device(br * 2.5e-3), ctx.to_device(bi * 2.5e-3)
+        s0 = ctx.stats()
+        xr, xi = ctx.zeros(), ctx.zeros()
+        ctx.minres_schro(dV, alpha, xr, xi, dbr, dbi, 200, 1e-30, x_is_zero=True)
+        torch.cuda.synchronize()
+        s1 = ctx.stats()
+        g_it = (s1.solver_kernel_ms - s0.solver_kernel_ms) / 1e3 / max(1, s1.solver_iterations_fp64 -
+                                                                       s0.solver_iterations_fp64)
+        out[name] = {"mesh": f"{n}x{n} quads, p = {p}", "reference_mesh_setup_s": setup,
+                     "reference_cpu_s_per_minres_iteration": t_it / cap, "sample_iterations": cap,
+                     "gpu_fp64_s_per_minres_iteration": g_it, "ratio": (t_it / cap) / g_it}
+        ctx.close()
+    print(json.dumps({"leg": "cpu", "metric": "reference OpenMP build vs GPU on the further configurations",
+                      **out}), flush=True)
+
+
 # ================================================================= c4: learned stage guess
 def c4_fields(X, Y, seed):
     """seed s: six Gaussians (amplitude U(-20,20), width U(0.3,1.5), centres
@@ -1231,7 +1321,7 @@ def main():
     ap.add_argument("--no-sweep", action="store_true", help="skip the p = 2..16 apply sweep")
     ap.add_argument("--forms", default="fp64,fp64_reftol,mixed,mixed_fdm,mixed_fdm_extrap,mixed_fdm_extrap2,"
                                        "mixed_fdm_learned,mixed_fdm_proj,mixed_fdm_proj_learned", help="solver forms to time (comma list)")
-    ap.add_argument("--leg", choices=["c4", "c5"], help="run one further workload instead of the headline")
+    ap.add_argument("--leg", choices=["c4", "c5", "cpu"], help="run one further workload instead of the headline")
     ap.add_argument("--c4-train", type=int, default=256)
     ap.add_argument("--c4-train-steps", type=int, default=50)
     ap.add_argument("--c4-eval", type=int, default=32)
@@ -1261,6 +1351,8 @@ def main():
         run_c4(args)
     elif args.leg == "c5":
         run_c5(args)
+    elif args.leg == "cpu":
+        run_cpu_legs(args)
     elif args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return

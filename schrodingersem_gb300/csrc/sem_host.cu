@@ -93,8 +93,8 @@ __global__ void k_to_f32(long long n, const double* __restrict__ a, float* __res
 constexpr int PROJ_MAX = 24;
 struct PtrList {
     int nz;
-    const double* z[PROJ_MAX];
-    double c[PROJ_MAX];
+    const double* z[PROJ_MAX + 1];
+    double c[PROJ_MAX + 1];
 };
 
 // per-block partial sums of b.b_j (j < L.nz) and b.b, laid out
@@ -131,14 +131,14 @@ __global__ void __launch_bounds__(256) k_multidot(long long n, const double* __r
     }
 }
 
-// out = sum_l c_l z_l over up to PROJ_MAX vectors
+// out = sum_l c_l z_l over up to PROJ_MAX + 1 vectors
 __global__ void k_lincomb_n(long long n, PtrList L, double* __restrict__ out)
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
          i += (long long)gridDim.x * blockDim.x) {
         double acc = 0.0;
 #pragma unroll
-        for (int l = 0; l < PROJ_MAX; ++l)
+        for (int l = 0; l <= PROJ_MAX; ++l)
             if (l < L.nz) acc = fma(L.c[l], __ldg(L.z[l] + i), acc);
         out[i] = acc;
     }
@@ -1814,12 +1814,27 @@ static int guess_residual(sem_ctx* c, const double* V, double alpha, const doubl
     return launch_learn_op(c, a);
 }
 
-static int norm2_planes(sem_ctx* c, const double* r, double* out)
+// (a.a, a.b, b.b) of two-plane vectors, owner-weighted, one synchronisation
+static int dots3(sem_ctx* c, const double* a, const double* b, double* aa, double* ab, double* bbv)
 {
-    double a1 = 0, a2 = 0;
-    int s = 0;
-    if ((s = dot_dev(c, r, r, &a1)) || (s = dot_dev(c, r + c->n, r + c->n, &a2))) return s;
-    *out = a1 + a2;
+    double* part = nullptr;
+    int s = wsget(c, "dot_part", 152 * 64, &part);
+    if (s) return s;
+    int used = 0;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dot3<decltype(nv)::value>(c->dm, a, b, part, 152 * 64 / 3, &used, c->stream);
+    }));
+    SEM_CUDA(cudaMemcpyAsync(c->h_part, part, sizeof(double) * 3 * used, cudaMemcpyDeviceToHost, c->stream));
+    SEM_CUDA(cudaStreamSynchronize(c->stream));
+    double s0 = 0, s1 = 0, s2 = 0;
+    for (int i = 0; i < used; ++i) {
+        s0 += c->h_part[3 * i];
+        s1 += c->h_part[3 * i + 1];
+        s2 += c->h_part[3 * i + 2];
+    }
+    if (aa) *aa = s0;
+    if (ab) *ab = s1;
+    if (bbv) *bbv = s2;
     return SEM_OK;
 }
 
@@ -1830,7 +1845,7 @@ static int norm2_planes(sem_ctx* c, const double* r, double* out)
 // fallback).  *zext receives a copy of the extrapolated guess (the base the
 // training targets are measured from).
 static int learned_guess(sem_ctx* c, const double* V, double alpha, const double* b, double* z, bool use,
-                         double** zext)
+                         double** zext, const double* rbase)
 {
     const int NN = c->N * c->N;
     double *r = nullptr, *zx = nullptr;
@@ -1842,9 +1857,12 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
         return s;
     SEM_CUDA(cudaMemcpyAsync(zx, z, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
     *zext = zx;
-    if ((s = guess_residual(c, V, alpha, b, zx, r))) return s;
+    if (rbase)  // the base guess's residual is known (projection): continuous copy
+        SEM_CUDA(cudaMemcpyAsync(r, rbase, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
+    else if ((s = guess_residual(c, V, alpha, b, zx, r)))
+        return s;
     double n_ext = 0;
-    if ((s = norm2_planes(c, r, &n_ext))) return s;
+    if ((s = dots3(c, r, r, &n_ext, nullptr, nullptr))) return s;
     LearnArgs a{};
     a.what = LEARN_FEATURES;
     a.r = r;
@@ -1874,11 +1892,8 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     // minimal residual along the predicted correction d = z_l - z_ext:
     // r(theta) = r_ext - theta A d with A d = r_ext - r_l, so
     // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|
-    double n_l = 0, x1 = 0, x2 = 0;
-    if ((s = norm2_planes(c, r2, &n_l)) || (s = dot_dev(c, r, r2, &x1)) ||
-        (s = dot_dev(c, r + c->n, r2 + c->n, &x2)))
-        return s;
-    const double rx = x1 + x2;
+    double n_l = 0, rx = 0;
+    if ((s = dots3(c, r, r2, nullptr, &rx, &n_l))) return s;
     const double den = n_ext - 2.0 * rx + n_l;
     double theta = den > 0 ? (n_ext - rx) / den : 0.0;
     // full step: the prediction as it is, unless it is not finite or raises
@@ -2022,7 +2037,7 @@ static int proj_dots(sem_ctx* c, const double* b, const double* slots, std::vect
 // residual |b - sum c_j b_j| / |b| in *ratio (1 when no basis direction is
 // kept, then x0 = 0)
 static int proj_guess(sem_ctx* c, const double* slots, const std::vector<double>& d, double bb, double* x0,
-                      double* ratio)
+                      double* ratio, std::vector<double>* coef)
 {
     const int k = c->proj_count;
     const int K = c->proj_k;
@@ -2058,6 +2073,30 @@ static int proj_guess(sem_ctx* c, const double* slots, const std::vector<double>
     c->stats.kernel_launches++;
     SEM_CUDA(cudaGetLastError());
     *ratio = bb > 0 ? std::sqrt(std::max(0.0, bb - cd) / bb) : 1.0;
+    if (coef) *coef = cf;
+    return SEM_OK;
+}
+
+// r = unmask(b - sum_j c_j b_j): the projection's residual in the continuous
+// format, without an operator apply (each stored pair meets A z_j = b_j to
+// the solver tolerance, far below the projection residual)
+static int proj_residual(sem_ctx* c, const double* slots, const std::vector<double>& cf, const double* b, double* r)
+{
+    PtrList L{};
+    L.nz = (int)cf.size() + 1;
+    L.z[0] = b;
+    L.c[0] = 1.0;
+    for (int j = 0; j < (int)cf.size(); ++j) {
+        L.z[j + 1] = slots + (size_t)j * 4 * c->n + 2 * c->n;
+        L.c[j + 1] = -cf[j];
+    }
+    k_lincomb_n<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, L, r);
+    c->stats.kernel_launches++;
+    SEM_CUDA(cudaGetLastError());
+    for (int q = 0; q < 2; ++q)
+        SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+            return launch_unmask<decltype(nv)::value>(c->dm, false, r + q * c->n, c->stream);
+        }));
     return SEM_OK;
 }
 
@@ -2178,12 +2217,14 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             auto hz = [&](long long back) {
                 return Zring + (size_t)((gstep - back) % RING) * zset + (size_t)st * 2 * c->n;
             };
-            std::vector<double> pd;
+            std::vector<double> pd, pcf;
             double pbb = 0.0;
+            bool projected = false;
             if (proj && (s = proj_dots(c, b, pslots, pd, &pbb))) return s;
             if (proj && c->proj_count > 0) {
                 double ratio = 1.0;
-                if ((s = proj_guess(c, pslots, pd, pbb, z, &ratio))) return s;
+                if ((s = proj_guess(c, pslots, pd, pbb, z, &ratio, &pcf))) return s;
+                projected = true;
                 c->stats.projected_guesses++;
                 c->stats.last_projection_ratio = ratio;
                 c->stats.projection_ratio_sum += ratio;
@@ -2220,7 +2261,12 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             const bool use = extrap && gstep >= 2 && !x_zero && c->guess == SEM_GUESS_LEARNED && c->learner;
             double* zext = nullptr;
             if (rec || use) {
-                if ((s = learned_guess(c, r.V, alpha, b, z, use, &zext))) return s;
+                double* rp = nullptr;
+                if (projected) {
+                    if ((s = wsget(c, "proj_r", 2 * c->n, &rp)) || (s = proj_residual(c, pslots, pcf, b, rp)))
+                        return s;
+                }
+                if ((s = learned_guess(c, r.V, alpha, b, z, use, &zext, rp))) return s;
             }
             sem_solver_results res{};
             int sw = 1;

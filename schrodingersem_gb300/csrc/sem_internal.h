@@ -194,6 +194,10 @@ cudaError_t launch_mask(const DevMesh& m, bool fp32, void* a, cudaStream_t st);
 template <int N>
 cudaError_t launch_dot(const DevMesh& m, const double* a, const double* b, double* part,
                        int max_blocks, int* blocks_used, cudaStream_t st);
+// (a.a, a.b, b.b) over both planes of two-plane vectors, 3 partials per block
+template <int N>
+cudaError_t launch_dot3(const DevMesh& m, const double* a, const double* b, double* part, int max_blocks,
+                        int* blocks_used, cudaStream_t st);
 // out[n] = gather(p + sum_l c[l] z_l) for every node (unmask semantics); then
 // optional f-apply: y = L-closure of the combination.
 struct ZList {

@@ -471,6 +471,49 @@ cudaError_t launch_mask(const DevMesh& m, bool fp32, void* a, cudaStream_t st)
     return cudaGetLastError();
 }
 
+// three owner-weighted dots of two-plane vectors at once: part[3 blk + q] =
+// (a.a, a.b, b.b) over both planes (fixed order)
+template <int N>
+__global__ void k_dot3(DevMesh m, const double* __restrict__ a, const double* __restrict__ b, double* part)
+{
+    __shared__ double red[34];
+    constexpr int NN = N * N;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0;
+    for (long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x; idx < m.n;
+         idx += (long long)gridDim.x * blockDim.x) {
+        const int e = (int)(idx / NN);
+        const int node = (int)(idx - (long long)e * NN);
+        const NodeInfo ni = node_info<N>(m, e, node % N, node / N);
+        if (ni_owner(ni)) {
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const double x = a[q * m.n + idx], y = b[q * m.n + idx];
+                s0 = fma(x, x, s0);
+                s1 = fma(x, y, s1);
+                s2 = fma(y, y, s2);
+            }
+        }
+    }
+    s0 = block_sum(s0, red);
+    s1 = block_sum(s1, red);
+    s2 = block_sum(s2, red);
+    if (threadIdx.x == 0) {
+        part[3 * blockIdx.x] = s0;
+        part[3 * blockIdx.x + 1] = s1;
+        part[3 * blockIdx.x + 2] = s2;
+    }
+}
+
+template <int N>
+cudaError_t launch_dot3(const DevMesh& m, const double* a, const double* b, double* part, int max_blocks,
+                        int* blocks_used, cudaStream_t st)
+{
+    const int grid = grid_for(m.n, 256, max_blocks);
+    *blocks_used = grid;
+    k_dot3<N><<<grid, 256, 0, st>>>(m, a, b, part);
+    return cudaGetLastError();
+}
+
 template <int N>
 cudaError_t launch_dot(const DevMesh& m, const double* a, const double* b, double* part,
                        int max_blocks, int* blocks_used, cudaStream_t st)
@@ -555,6 +598,8 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
     template cudaError_t launch_mask<NV>(const DevMesh&, bool, void*, cudaStream_t);                 \
     template cudaError_t launch_dot<NV>(const DevMesh&, const double*, const double*, double*, int,  \
                                         int*, cudaStream_t);                                         \
+    template cudaError_t launch_dot3<NV>(const DevMesh&, const double*, const double*, double*, int, \
+                                         int*, cudaStream_t);                                        \
     template cudaError_t launch_combo_f<NV>(const DevMesh&, const double*, const double*,            \
                                             const ZList&, double*, cudaStream_t);                    \
     template cudaError_t launch_update<NV>(const DevMesh&, const double*, const ZList&, double*,     \
