@@ -366,6 +366,16 @@ int sem_learner_fit(sem_learner* learner, const void* X, const float* T, long lo
 /* C (M x N FP32) = A (M x K BF16) B (K x N BF16), row-major device arrays,
  * the network's tensor-core GEMM */
 int sem_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, void* cuda_stream);
+/* (no counterpart in the reference) Tensor-core instruction path of every
+ * GEMM of the learned-guess network and of sem_gemm_bf16, process-wide:
+ * 1 (default) tcgen05.mma with the accumulator in tensor memory (M = 128
+ * per CTA, BF16 operands from shared memory, FP32 accumulation), 0 the
+ * warp-level mma.sync m16n8k16 kernel.  Both compute in BF16 x BF16 -> FP32. */
+int sem_gemm_set_path(int path);
+/* (no counterpart in the reference) *expired = 1 when a bounded wait of a
+ * tcgen05 GEMM ever ran out in this process (its output tile was then left
+ * unwritten); 0 otherwise */
+int sem_gemm_check_error(int* expired);
 /* network used by the SDIRK drivers when SEM_OPT_STAGE_GUESS is
  * SEM_GUESS_LEARNED in mixed precision (NULL: extrapolation only).  The
  * caller keeps ownership.  Every proposed guess is checked in FP64: the

@@ -108,6 +108,8 @@ SIGNATURES = {
     "sem_learner_get_grads": (C.c_int, [_vp, C.c_int, _vp, _vp]),
     "sem_learner_fit": (C.c_int, [_vp, _vp, _vp, C.c_longlong, C.c_int, C.c_int, C.c_float, C.c_ulonglong, _dp]),
     "sem_gemm_bf16": (C.c_int, [C.c_int, C.c_int, C.c_int, _vp, _vp, _vp, _vp]),
+    "sem_gemm_set_path": (C.c_int, [C.c_int]),
+    "sem_gemm_check_error": (C.c_int, [C.POINTER(C.c_int)]),
     "sem_ctx_set_learner": (C.c_int, [_vp, _vp]),
     "sem_batch_create": (C.c_int, [C.POINTER(_vp), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                    C.POINTER(_vp), C.POINTER(C.c_int), C.POINTER(_vp), C.c_uint]),

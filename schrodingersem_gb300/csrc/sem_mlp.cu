@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "sem_gb300.h"
+#include "sem_apply_bulk.cuh"  // mbarrier helpers
 #include "sem_device.cuh"
 #include "sem_internal.h"
 
@@ -137,11 +138,250 @@ __global__ void __launch_bounds__(128) k_gemm_bf16(GemmArgs g)
                 }
 }
 
+// ------------------------------------------------ tcgen05 (5th-generation) GEMM
+// The same GEMM on the sm_100-family tensor cores: tcgen05.mma kind::f16
+// (BF16 A and B, FP32 accumulator in tensor memory), M = 128 rows per CTA,
+// N = TC_BN columns, K in steps of 16 from shared-memory operands staged by
+// the CTA's 128 threads (generic strides, FP32 or BF16 sources converted to
+// BF16, zero-filled past the matrix edges) in the canonical K-major layout
+// without swizzle: 8-row x 16-byte core matrices, the two core matrices of a
+// 16-wide K step 128 bytes apart (leading-dimension offset), consecutive
+// 8-row groups 256 bytes apart (stride-dimension offset).  Two K tiles of 64
+// are staged alternately: the loads of tile k+1 overlap the MMAs of tile k,
+// and a tile's buffer is reused only after the mbarrier its commit arrives on
+// has completed.  One thread issues the MMAs; the four warps then read the
+// accumulator rows they own (TMEM lanes 32w..32w+31) with tcgen05.ld and run
+// the epilogue.  Every wait is bounded; the CTA always frees its tensor
+// memory before it returns.
+constexpr int TC_M = 128, TC_BK = 64, TC_THREADS = 128;
+__device__ int g_tc_err;  // set when a bounded wait of k_gemm_tc expired
+
+__host__ __device__ constexpr uint32_t tc_idesc(int m, int n)
+{
+    return (1u << 4)                         // accumulator: FP32
+           | (1u << 7)                       // A: BF16
+           | (1u << 10)                      // B: BF16 (both K-major, not negated)
+           | ((uint32_t)(n >> 3) << 17)      // N / 8
+           | ((uint32_t)(m >> 4) << 24);     // M / 16
+}
+
+__device__ __forceinline__ uint64_t tc_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo)
+{
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);  // version 1, no swizzle
+}
+
+// byte offset of (row r, k) in a staged tile of R rows x TC_BK
+__device__ __forceinline__ uint32_t tc_off(int R, int r, int k)
+{
+    return (uint32_t)((k >> 4) * (R * 32) + (r >> 3) * 256 + ((k >> 3) & 1) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// 8 consecutive values of one operand row (K-contiguous when stride 1),
+// packed as 4 BF16 pairs; vector loads when the row run is aligned and in range
+__device__ __forceinline__ void tc_chunk(const void* X, int bf, long long base, long long sk, int kvalid,
+                                         uint32_t (&w)[4])
+{
+    if (sk == 1 && kvalid >= 8) {
+        if (bf) {
+            const __nv_bfloat16* p = (const __nv_bfloat16*)X + base;
+            const uintptr_t a = (uintptr_t)p;
+            if ((a & 15) == 0) {
+                const uint4 v = __ldg((const uint4*)p);
+                w[0] = v.x; w[1] = v.y; w[2] = v.z; w[3] = v.w;
+                return;
+            }
+            if ((a & 7) == 0) {
+                const uint2 v0 = __ldg((const uint2*)p), v1 = __ldg((const uint2*)p + 1);
+                w[0] = v0.x; w[1] = v0.y; w[2] = v1.x; w[3] = v1.y;
+                return;
+            }
+            if ((a & 3) == 0) {
+#pragma unroll
+                for (int h = 0; h < 4; ++h) w[h] = __ldg((const unsigned int*)p + h);
+                return;
+            }
+        } else {
+            const float* p = (const float*)X + base;
+            if (((uintptr_t)p & 15) == 0) {
+                const float4 v0 = __ldg((const float4*)p), v1 = __ldg((const float4*)p + 1);
+                w[0] = pack_bf16(__float2bfloat16(v0.x), __float2bfloat16(v0.y));
+                w[1] = pack_bf16(__float2bfloat16(v0.z), __float2bfloat16(v0.w));
+                w[2] = pack_bf16(__float2bfloat16(v1.x), __float2bfloat16(v1.y));
+                w[3] = pack_bf16(__float2bfloat16(v1.z), __float2bfloat16(v1.w));
+                return;
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 4; ++h) {
+        const float v0 = (2 * h < kvalid) ? ld_any(X, base + (long long)(2 * h) * sk, bf) : 0.f;
+        const float v1 = (2 * h + 1 < kvalid) ? ld_any(X, base + (long long)(2 * h + 1) * sk, bf) : 0.f;
+        w[h] = pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
+    }
+}
+
+template <int BN>
+__device__ __forceinline__ void tc_stage(const GemmArgs& g, unsigned char* sA, unsigned char* sB, int m0, int n0,
+                                         int k0)
+{
+    // 16-byte chunks: 8 consecutive k of one row; every thread issues all of
+    // its chunks' loads before its shared-memory stores
+    constexpr int NQ = ((TC_M + BN) * (TC_BK / 8) + TC_THREADS - 1) / TC_THREADS;
+    uint32_t w[NQ][4];
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        const int q = threadIdx.x + i * TC_THREADS;
+        const bool isA = q < TC_M * (TC_BK / 8);
+        const int qq = isA ? q : q - TC_M * (TC_BK / 8);
+        const int r = qq >> 3, kc = qq & 7;
+        const int k = k0 + kc * 8;
+        const int row = (isA ? m0 : n0) + r;
+        const bool in = isA ? (row < g.M) : (row < g.N);
+        const int kvalid = in ? min(8, g.K - k) : 0;
+        if (kvalid <= 0) {
+            w[i][0] = w[i][1] = w[i][2] = w[i][3] = 0u;
+            continue;
+        }
+        if (isA)
+            tc_chunk(g.A, g.a_bf16, (long long)row * g.sa_m + (long long)k * g.sa_k, g.sa_k, kvalid, w[i]);
+        else
+            tc_chunk(g.B, g.b_bf16, (long long)k * g.sb_k + (long long)row * g.sb_n, g.sb_k, kvalid, w[i]);
+    }
+#pragma unroll
+    for (int i = 0; i < NQ; ++i) {
+        const int q = threadIdx.x + i * TC_THREADS;
+        const bool isA = q < TC_M * (TC_BK / 8);
+        const int qq = isA ? q : q - TC_M * (TC_BK / 8);
+        const int r = qq >> 3, kc = qq & 7;
+        unsigned char* dst = (isA ? sA + tc_off(TC_M, r, kc * 8) : sB + tc_off(BN, r, kc * 8));
+        *(uint4*)dst = make_uint4(w[i][0], w[i][1], w[i][2], w[i][3]);
+    }
+}
+
+template <int BN>
+__global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long timeout_ns)
+{
+    extern __shared__ __align__(1024) unsigned char tsm[];
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t tmem_base;
+    constexpr int ABYTES = TC_M * TC_BK * 2, BBYTES = BN * TC_BK * 2;
+    unsigned char* sA[2] = {tsm, tsm + ABYTES + BBYTES};
+    unsigned char* sB[2] = {tsm + ABYTES, tsm + 2 * ABYTES + BBYTES};
+    const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * BN;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(BN)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    constexpr uint32_t idesc = tc_idesc(TC_M, BN);
+    const int nk = (g.K + TC_BK - 1) / TC_BK;
+    bool ok = true;
+    for (int kt = 0; kt < nk && ok; ++kt) {
+        const int b = kt & 1;
+        if (kt >= 2) ok = mbar_wait(&bar[b], (uint32_t)(((kt - 2) >> 1) & 1), timeout_ns);
+        if (!__syncthreads_and(ok)) {
+            ok = false;
+            break;
+        }
+        tc_stage<BN>(g, sA[b], sB[b], m0, n0, kt * TC_BK);
+        fence_proxy_async_smem();  // the staged tile is read by the tensor cores (async proxy)
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t a0 = smem_addr(sA[b]), b0 = smem_addr(sB[b]);
+#pragma unroll
+            for (int ks = 0; ks < TC_BK / 16; ++ks) {
+                const uint64_t ad = tc_desc(a0 + ks * TC_M * 32, 128, 256);
+                const uint64_t bd = tc_desc(b0 + ks * BN * 32, 128, 256);
+                const uint32_t acc = (kt > 0 || ks > 0) ? 1u : 0u;
+                asm volatile(
+                    "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                    "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(taddr),
+                    "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+                    : "memory");
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&bar[b]))
+                         : "memory");
+        }
+    }
+    if (ok && nk > 0) ok = mbar_wait(&bar[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1), timeout_ns);
+    ok = __syncthreads_and(ok) != 0;
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    if (ok) {
+        const int m = m0 + warp * 32 + lane;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            if (m < g.M) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int nn = n0 + c0 + j;
+                    if (nn >= g.N) continue;
+                    float v = __uint_as_float(r[j]);
+                    if (g.accumulate) v += g.C[(long long)m * g.ldc + nn];
+                    if (g.bias) v += g.bias[nn];
+                    if (g.relu) v = fmaxf(v, 0.f);
+                    g.C[(long long)m * g.ldc + nn] = v;
+                    if (g.Cbf) g.Cbf[(long long)m * g.ldc + nn] = __float2bfloat16(v);
+                }
+            }
+        }
+    } else if (threadIdx.x == 0) {
+        atomicExch(&g_tc_err, 1);
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(BN) : "memory");
+}
+
+// GEMM path: 1 (default) the tcgen05 kernel, 0 the warp-level mma.sync kernel
+int g_gemm_path = 1;
+
 cudaError_t gemm(const GemmArgs& g, cudaStream_t st)
 {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) return cudaSuccess;
-    dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M);
-    k_gemm_bf16<<<grid, 128, 0, st>>>(g);
+    if (g_gemm_path == 0) {
+        dim3 grid((g.N + GT_N - 1) / GT_N, (g.M + GT_M - 1) / GT_M);
+        k_gemm_bf16<<<grid, 128, 0, st>>>(g);
+        return cudaGetLastError();
+    }
+    const long long tmo = 2000000000LL;  // 2 s
+    // 64-column tiles when 128-column ones would leave most SMs idle
+    const long long mt = (g.M + TC_M - 1) / TC_M;
+    if (g.N <= 64 || mt * ((g.N + 127) / 128) < 152) {
+        constexpr size_t smem = 2 * (size_t)(TC_M + 64) * TC_BK * 2;
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<64>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc<64><<<dim3((g.N + 63) / 64, (g.M + TC_M - 1) / TC_M), TC_THREADS, smem, st>>>(g, tmo);
+    } else {
+        constexpr size_t smem = 2 * (size_t)(TC_M + 128) * TC_BK * 2;
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<128>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc<128><<<dim3((g.N + 127) / 128, (g.M + TC_M - 1) / TC_M), TC_THREADS, smem, st>>>(g, tmo);
+    }
     return cudaGetLastError();
 }
 
@@ -199,6 +439,17 @@ __global__ void k_to_bf16(long long n, const float* __restrict__ a, __nv_bfloat1
         b[i] = __float2bfloat16(a[i]);
 }
 
+// wt[o][i] = w[i][o] (BF16, rows x cols -> cols x rows)
+__global__ void k_transpose_bf16(int rows, int cols, const __nv_bfloat16* __restrict__ w,
+                                 __nv_bfloat16* __restrict__ wt)
+{
+    const long long n = (long long)rows * cols;
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+        const int o = (int)(t / rows), i = (int)(t - (long long)o * rows);
+        wt[t] = w[(long long)i * cols + o];
+    }
+}
+
 int g1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 4096); }
 
 }  // namespace
@@ -209,6 +460,11 @@ struct sem_learner {
     // parameters: FP32 master, BF16 copies for the GEMMs, Adam moments, gradients
     float *W[3] = {}, *b[3] = {}, *gW[3] = {}, *gb[3] = {}, *mW[3] = {}, *vW[3] = {}, *mb[3] = {}, *vb[3] = {};
     __nv_bfloat16* Wbf[3] = {};
+    // transposed BF16 copies [out][in] for the forward GEMMs (their K runs
+    // contiguous, so the tensor-core operand staging uses vector loads);
+    // rebuilt before a forward pass whenever the weights changed
+    __nv_bfloat16* WbfT[3] = {};
+    bool wt_dirty = true;
     int rows_cap = 0;
     float *h1 = nullptr, *h2 = nullptr, *out = nullptr, *d2 = nullptr, *d1 = nullptr, *dout = nullptr;
     __nv_bfloat16 *h1bf = nullptr, *h2bf = nullptr;
@@ -281,6 +537,7 @@ extern "C" int sem_learner_create(sem_learner** out, int d_in, int hidden, int d
         float** bb[] = {&L->b[l], &L->gb[l], &L->mb[l], &L->vb[l]};
         for (float** p : bb) LCUDA(cudaMalloc(p, nb * 4));
         LCUDA(cudaMalloc(&L->Wbf[l], nw * 2));
+        LCUDA(cudaMalloc(&L->WbfT[l], nw * 2));
         LCUDA(cudaMemcpy(L->W[l], w.data(), nw * 4, cudaMemcpyHostToDevice));
         LCUDA(cudaMemset(L->mW[l], 0, nw * 4));
         LCUDA(cudaMemset(L->vW[l], 0, nw * 4));
@@ -304,6 +561,7 @@ extern "C" int sem_learner_destroy(sem_learner* L)
         for (float* p : f)
             if (p) cudaFree(p);
         if (L->Wbf[l]) cudaFree(L->Wbf[l]);
+        if (L->WbfT[l]) cudaFree(L->WbfT[l]);
     }
     float* f2[] = {L->h1, L->h2, L->out, L->d2, L->d1, L->dout};
     for (float* p : f2)
@@ -348,6 +606,7 @@ extern "C" int sem_learner_set_params(sem_learner* L, int l, const float* W, con
     if (W) {
         LCUDA(cudaMemcpy(L->W[l], W, nw * 4, cudaMemcpyHostToDevice));
         k_to_bf16<<<g1d(nw), 256, 0, L->stream>>>(nw, L->W[l], L->Wbf[l]);
+        L->wt_dirty = true;
         LCUDA(cudaGetLastError());
     }
     if (b) LCUDA(cudaMemcpy(L->b[l], b, (size_t)L->dout_(l) * 4, cudaMemcpyHostToDevice));
@@ -360,16 +619,25 @@ static int forward(sem_learner* L, int rows, const __nv_bfloat16* x)
 {
     int s = ensure_rows(L, rows);
     if (s) return s;
+    if (L->wt_dirty) {
+        for (int l = 0; l < 3; ++l) {
+            const long long nw = (long long)L->din(l) * L->dout_(l);
+            k_transpose_bf16<<<g1d(nw), 256, 0, L->stream>>>(L->din(l), L->dout_(l), L->Wbf[l], L->WbfT[l]);
+        }
+        LCUDA(cudaGetLastError());
+        L->wt_dirty = false;
+    }
+    // B(k, n) = W[k][n] = WT[n][k]: K contiguous
     GemmArgs g{};
     g.M = rows; g.N = L->H; g.K = L->d_in;
     g.A = x; g.sa_m = L->d_in; g.sa_k = 1; g.a_bf16 = 1;
-    g.B = L->Wbf[0]; g.sb_k = L->H; g.sb_n = 1; g.b_bf16 = 1;
+    g.B = L->WbfT[0]; g.sb_k = 1; g.sb_n = L->d_in; g.b_bf16 = 1;
     g.C = L->h1; g.ldc = L->H; g.bias = L->b[0]; g.relu = 1; g.Cbf = L->h1bf;
     LCUDA(gemm(g, L->stream));
     g.K = L->H; g.A = L->h1bf; g.sa_m = L->H;
-    g.B = L->Wbf[1]; g.C = L->h2; g.bias = L->b[1]; g.Cbf = L->h2bf;
+    g.B = L->WbfT[1]; g.sb_n = L->H; g.C = L->h2; g.bias = L->b[1]; g.Cbf = L->h2bf;
     LCUDA(gemm(g, L->stream));
-    g.N = L->d_out; g.A = L->h2bf; g.B = L->Wbf[2]; g.sb_k = L->d_out;
+    g.N = L->d_out; g.A = L->h2bf; g.B = L->WbfT[2]; g.sb_n = L->H;
     g.C = L->out; g.ldc = L->d_out; g.bias = L->b[2]; g.relu = 0; g.Cbf = nullptr;
     LCUDA(gemm(g, L->stream));
     return SEM_OK;
@@ -439,6 +707,7 @@ extern "C" int sem_learner_train_step(sem_learner* L, int rows, const void* x_bf
     LCUDA(cudaGetLastError());
     if (lr > 0.f) {
         ++L->adam_t;
+        L->wt_dirty = true;
         const float b1 = 0.9f, b2 = 0.999f;
         const float c1 = 1.f - std::pow(b1, (float)L->adam_t), c2 = 1.f - std::pow(b2, (float)L->adam_t);
         for (int l = 0; l < 3; ++l) {
@@ -532,6 +801,23 @@ extern "C" int sem_learner_fit(sem_learner* L, const void* X, const float* T, lo
     cudaFree(Tb);
     if (status) return status;
     if (final_loss) *final_loss = last;
+    return SEM_OK;
+}
+
+extern "C" int sem_gemm_set_path(int path)
+{
+    if (path != 0 && path != 1) return ctx_fail(SEM_ERR_ARG, "gemm path must be 0 (mma.sync) or 1 (tcgen05)");
+    g_gemm_path = path;
+    return SEM_OK;
+}
+
+extern "C" int sem_gemm_check_error(int* expired)
+{
+    if (!expired) return ctx_fail(SEM_ERR_ARG, "null argument");
+    int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, g_tc_err, sizeof(int));
+    if (e != cudaSuccess) return ctx_fail(SEM_ERR_CUDA, cudaGetErrorString(e));
+    *expired = v;
     return SEM_OK;
 }
 
