@@ -55,11 +55,12 @@ WORKLOAD = ("Schroedinger SDIRK4-3 time step, 64x64 jittered quads on [-8,8]^2 (
             "MINRES tol 1e-10")
 DT, TOL, P, NEL = 1e-2, 1e-10, 8, 64
 ORACLE_TOL = 1e-13  # MINRES tolerance of the FP64 accuracy reference runs
-# DRAM bytes (read + write) per launch of the element-preconditioned FP32
-# solver kernel on this workload, from the ncu capture summarised in
-# profiles/launches_sdirk4s3_64x64_p8_learned_fp32.md (mean of three launches
-# of the timed steps).  The solver's working set stays in L2.
-SOLVER_DRAM_BYTES_PER_LAUNCH = 90.8e6
+# DRAM bytes (read + write) per launch of the on-chip resident solver kernel
+# (k_minres_resident<9>) inside the timed steps of the headline form: ncu
+# capture summarised in profiles/k_minres_resident_64x64_p8.md (mean of three
+# launches).  The Krylov vectors stay on chip; these bytes are the FP64
+# refinement's fields and the per-launch loads.
+SOLVER_DRAM_BYTES_PER_LAUNCH = 41.24e6
 APPLY_NEL = 559  # 559^2 elements at p = 8: 4473^2 = 20.0 M global nodes
 
 
@@ -911,8 +912,9 @@ def run_ours(args):
                          "speedup_vs_plain_fp64": (res[plain]["ms"] / res[best]["ms"]) if plain else None},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": (achieved / hbm_peak) if achieved else None,
-                     "traffic": SOLVER_DRAM_BYTES_PER_LAUNCH if FORMS[head][2] == 2 and prec == "mixed" else None,
-                     "traffic_source": "ncu capture of the timed steps' solver launches (constant in this file)",
+                     "traffic": SOLVER_DRAM_BYTES_PER_LAUNCH if resident else None,
+                     "traffic_source": "ncu capture of the timed steps' solver launches (constant in this file, "
+                                       "profiles/k_minres_resident_64x64_p8.md)",
                      "algorithmic_bytes_per_launch": alg_bytes / max(1, H["solver_launches"]),
                      "launches": H["solver_launches"],
                      "kernel": kern + " (persistent cooperative solver)",
@@ -966,9 +968,10 @@ def run_cpu_legs(a):
     jittered 0.15h seed 0, p = 4, PCG 1e-12), the Res apply (64x64 quads,
     p = 8, algorithmic bytes 9 words/node), and bounded MINRES samples of the
     c4 (128x128, p = 8) and c5 (384x384, p = 12) stage solves: seconds per
-    reference MINRES iteration on the stage operator (capped sample), next
-    to the GPU's plain FP64 MINRES seconds per iteration on the same
-    operator.  One JSON line."""
+    MINRES iteration on the stage operator (capped sample; on the oracle
+    restatement, the reference's loader overflows on these meshes), next to
+    the GPU's plain FP64 MINRES seconds per iteration on the same operator.
+    One JSON line."""
     import torch
 
     import schrodingersem_gb300 as S
@@ -1009,23 +1012,41 @@ def run_cpu_legs(a):
     out["apply"] = {"mesh": "64x64 quads, p = 8 (331,776 element-local nodes per component)",
                     "reference_cpu_s": t_app, "reference_cpu_gbs_algorithmic": nloc * 8 * 9 / t_app / 1e9,
                     "note": "FP64, 9 words/node; includes the reference's unmask/global_sum/mask"}
-    # ---- bounded MINRES samples of the c4 / c5 stage operators
+    # ---- bounded MINRES samples of the c4 / c5 stage operators.  The
+    # reference's load_mesh cannot read these meshes: its edge key inversion
+    # (include/load_mesh.hpp:24-30) evaluates 8*z+1 in int, which overflows
+    # once two corner ids sum above about 23,170 (the 128x128 mesh has
+    # 16,641 corners), so the samples run on the oracle restatement (the
+    # same algorithm, bit-identical to the reference where both run)
+    from oracle import oracle as O
+    O.set_threads(threads)
     for name, n, p, box, cap in (("c4", 128, 8, 10.0, 30), ("c5", 384, 12, 12.0, 4)):
         co, el = structured_quads(n, box=(-box, box, -box, box), jitter=0.1, seed=1)
+        try:
+            _ref_mesh(R, p, co, el)
+            ref_loads = True
+        except Exception as e:  # the overflow above
+            ref_loads = str(e).splitlines()[0][:160]
         t0 = time.perf_counter()
-        rm = _ref_mesh(R, p, co, el)
+        om = O.Mesh(p, coords=co, elements=el)
         setup = time.perf_counter() - t0
-        X, Y = rm.node_coords()
+        X, Y = om.node_coords()
         V = 0.5 * (X * X + Y * Y)
-        br, bi = rm.schro_f(V, np.exp(-X * X - Y * Y), np.zeros_like(X))
+        br, bi = om.schro_f(V, np.exp(-X * X - Y * Y), np.zeros_like(X))
+        br, bi = br * 2.5e-3, bi * 2.5e-3
         alpha = 0.25 * 2.5e-3
-        t_it, _ = _timed(lambda: rm.minres_res(V, alpha, br * 2.5e-3, bi * 2.5e-3, rm.zeros(), rm.zeros(), cap,
-                                               1e-30))
-        del rm
+        nn = om.n_el * om.N * om.N
+        apply = lambda v: np.concatenate([t.ravel() for t in om.schro_res(  # noqa: E731
+            V, alpha, v[:nn].reshape(om.shape), v[nn:].reshape(om.shape))])
+        dot = lambda u, v: om.dot(u[:nn].reshape(om.shape), v[:nn].reshape(om.shape)) + \
+            om.dot(u[nn:].reshape(om.shape), v[nn:].reshape(om.shape))  # noqa: E731
+        bvec = np.concatenate([br.ravel(), bi.ravel()])
+        t_it, _ = _timed(lambda: O.krylov("minres", apply, bvec, np.zeros_like(bvec), cap, 1e-30, dot))
+        del om
         ctx = S.Context(p, coords=co, elements=el)
         ctx.set_option(capi.OPT_PROFILE, 1)
         dV = ctx.to_device(V)
-        dbr, dbi = ctx.to_device(br * 2.5e-3), ctx.to_device(bi * 2.5e-3)
+        dbr, dbi = ctx.to_device(br), ctx.to_device(bi)
         s0 = ctx.stats()
         xr, xi = ctx.zeros(), ctx.zeros()
         ctx.minres_schro(dV, alpha, xr, xi, dbr, dbi, 200, 1e-30, x_is_zero=True)
@@ -1033,8 +1054,9 @@ def run_cpu_legs(a):
         s1 = ctx.stats()
         g_it = (s1.solver_kernel_ms - s0.solver_kernel_ms) / 1e3 / max(1, s1.solver_iterations_fp64 -
                                                                        s0.solver_iterations_fp64)
-        out[name] = {"mesh": f"{n}x{n} quads, p = {p}", "reference_mesh_setup_s": setup,
-                     "reference_cpu_s_per_minres_iteration": t_it / cap, "sample_iterations": cap,
+        out[name] = {"mesh": f"{n}x{n} quads, p = {p}", "cpu_kind": "port",
+                     "reference_load_mesh": ref_loads, "oracle_mesh_setup_s": setup,
+                     "cpu_s_per_minres_iteration": t_it / cap, "sample_iterations": cap,
                      "gpu_fp64_s_per_minres_iteration": g_it, "ratio": (t_it / cap) / g_it}
         ctx.close()
     print(json.dumps({"leg": "cpu", "metric": "reference OpenMP build vs GPU on the further configurations",
@@ -1227,10 +1249,25 @@ def run_c5(a):
                                f"{a.c5_err:g}, MINRES 1e-10, FP32 inner + FP64 refinement, element preconditioner, "
                                f"extrapolated stage guess", "local_nodes_per_component": ctx.n},
     }
-    del dre, dim, dV
+    # the first accepted step again with the plain FP64 solver (zero stage
+    # guess, MINRES tolerance 1e-13, the reference's algorithm, pinned to the
+    # reference's outputs by the parity tests) at the same dt
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_FP64)
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_ZERO)
+    ctx.set_option(capi.OPT_PRECOND, capi.PRECOND_NONE)
+    t3 = time.time()
+    rr, ri = ctx.to_device(re), ctx.to_device(im)
+    okr = ctx.schrodinger("dirk4s5", rr, ri, dV, 0.5 * first[2], first[2], 40 * ctx.dof(), 1e-13)
+    pr, pi = rr.cpu().numpy(), ri.cpu().numpy()
+    out["fp64_replay"] = {"dt_workload_units": 2 * first[2], "converged": bool(okr), "gpu_s": time.time() - t3,
+                          "rel_err_first_step_vs_fp64": mass_norm(J, w, first[0] - pr, first[1] - pi) /
+                          mass_norm(J, w, pr, pi),
+                          "note": "the GPU's plain FP64 MINRES (the reference's algorithm, tolerance 1e-13) "
+                                  "replays the first accepted step with the same dt"}
+    del dre, dim, dV, rr, ri
     ctx.close()
     torch.cuda.empty_cache()
-    if not a.no_cpu:
+    if a.c5_cpu_replay:
         from oracle import oracle as O
         O.set_threads(cpu_threads())
         om = O.Mesh(p, coords=co, elements=el)
@@ -1334,6 +1371,8 @@ def main():
     ap.add_argument("--c5-steps", type=int, default=500)
     ap.add_argument("--c5-dt0", type=float, default=4e-4)
     ap.add_argument("--c5-err", type=float, default=1e-8)
+    ap.add_argument("--c5-cpu-replay", action="store_true",
+                    help="also replay the first accepted step on the CPU oracle (hours at the full size)")
     ap.add_argument("--profile-case", choices=["minres", "apply", "batch"])
     ap.add_argument("--pc-n", type=int, default=192)
     ap.add_argument("--pc-p", type=int, default=8)
