@@ -985,6 +985,7 @@ def run_cpu_legs(a):
     threads = cpu_threads()
     R.set_threads(threads)
     out = {"threads": threads}
+    print("cpu leg: c1", file=sys.stderr, flush=True)
     # ---- c1
     co, el = structured_quads(16, box=(0.0, 1.0, 0.0, 1.0), jitter=0.15, seed=0)
     rm = _ref_mesh(R, 4, co, el)
@@ -1001,6 +1002,7 @@ def run_cpu_legs(a):
                  "reference_iterations": it_r, "gpu": t_gpu, "gpu_iterations": it_g, "speedup": t_ref / t_gpu}
     ctx.close()
     # ---- Res apply at the c2 mesh
+    print("cpu leg: apply", file=sys.stderr, flush=True)
     co, el = workload_inputs()
     rm = _ref_mesh(R, P, co, el)
     X, Y = rm.node_coords()
@@ -1021,12 +1023,13 @@ def run_cpu_legs(a):
     from oracle import oracle as O
     O.set_threads(threads)
     for name, n, p, box, cap in (("c4", 128, 8, 10.0, 30), ("c5", 384, 12, 12.0, 4)):
+        print(f"cpu leg: {name}", file=sys.stderr, flush=True)
         co, el = structured_quads(n, box=(-box, box, -box, box), jitter=0.1, seed=1)
-        try:
-            _ref_mesh(R, p, co, el)
-            ref_loads = True
-        except Exception as e:  # the overflow above
-            ref_loads = str(e).splitlines()[0][:160]
+        # the largest edge key of the reference's Cantor pairing: 8 z + 1 must fit in int
+        ends = np.stack([el, np.roll(el, -1, axis=1)], axis=-1).reshape(-1, 2).astype(np.int64)
+        a_, b_ = ends.min(axis=1), ends.max(axis=1)
+        zmax = int((((a_ + b_) * (a_ + b_ + 1)) // 2 + b_).max())
+        ref_loads = 8 * zmax + 1 <= 2 ** 31 - 1  # not called when it would overflow (undefined behaviour)
         t0 = time.perf_counter()
         om = O.Mesh(p, coords=co, elements=el)
         setup = time.perf_counter() - t0
@@ -1055,7 +1058,8 @@ def run_cpu_legs(a):
         g_it = (s1.solver_kernel_ms - s0.solver_kernel_ms) / 1e3 / max(1, s1.solver_iterations_fp64 -
                                                                        s0.solver_iterations_fp64)
         out[name] = {"mesh": f"{n}x{n} quads, p = {p}", "cpu_kind": "port",
-                     "reference_load_mesh": ref_loads, "oracle_mesh_setup_s": setup,
+                     "reference_load_mesh_fits_int": ref_loads, "max_edge_key": zmax,
+                     "oracle_mesh_setup_s": setup,
                      "cpu_s_per_minres_iteration": t_it / cap, "sample_iterations": cap,
                      "gpu_fp64_s_per_minres_iteration": g_it, "ratio": (t_it / cap) / g_it}
         ctx.close()
