@@ -463,9 +463,13 @@ def run_batch(n_instances=1024, steps=100, warmup=3, seed=2026, rank=0, world=1,
 
 
 # ================================================================= apply, sweep, peaks
-def measure_apply(ctx, torch, prec, flush, reps):
+def measure_apply(ctx, torch, prec, flush, reps, pipeline=1):
     """device ms of one standalone Res apply (element kernel + assembly into
-    the masked format), L2 flushed before each, median of reps"""
+    the masked format), L2 flushed before each, median of reps; pipeline:
+    the FP32 element kernel (1 stored factors, 2 factors computed from the
+    element corners)"""
+    from schrodingersem_gb300 import capi
+    ctx.set_option(capi.OPT_APPLY_PIPELINE, pipeline)
     dt = torch.float64 if prec == "fp64" else torch.float32
     g = torch.Generator(device="cuda").manual_seed(ctx.N)
     q = [torch.randn(ctx.shape, dtype=dt, device="cuda", generator=g) for _ in range(3)]
@@ -504,10 +508,22 @@ def apply_leg(S, torch, fp64_peak, hbm_peak, reps=20):
         out[prec] = {"ms": ms, "gbs": nb / ms / 1e6, "bytes": nb, "tflops": fl / ms / 1e9, "flops": fl}
     out["fp32"]["frac_hbm"] = out["fp32"]["gbs"] / hbm_peak
     out["fp64"]["frac_fp64_pipe"] = out["fp64"]["tflops"] / fp64_peak if fp64_peak else None
+    out["fp32_geo"] = geo_row(ctx, measure_apply(ctx, torch, "fp32", flush, reps, pipeline=2), hbm_peak)
+    out["fp32_geo"]["speedup_vs_stored_factors"] = out["fp32"]["ms"] / out["fp32_geo"]["ms"]
     ctx.close()
     del flush
     torch.cuda.empty_cache()
     return out
+
+
+def geo_row(ctx, ms, hbm_peak):
+    """the FP32 Res apply with on-the-fly geometric factors: it moves
+    n_loc * 4 * 5 bytes (psi 2 planes, out 2, V) + 32 bytes of corner
+    differences per element; gbs_equivalent counts the 9 words of the
+    stored-factor apply (the same operator result per node)"""
+    nb = ctx.n * 4 * 5 + ctx.E * 32
+    return {"ms": ms, "bytes": nb, "gbs": nb / ms / 1e6, "frac_hbm": nb / ms / 1e6 / hbm_peak,
+            "gbs_equivalent": ctx.n * 4 * 9 / ms / 1e6, "gnodes_per_s": ctx.n / ms / 1e6}
 
 
 def sweep_leg(S, torch, hbm_peak, fp64_peak, degrees=range(2, 17), nodes=2e7, reps=5):
@@ -528,6 +544,10 @@ def sweep_leg(S, torch, hbm_peak, fp64_peak, degrees=range(2, 17), nodes=2e7, re
             row[prec] = {"ms": round(ms, 4), "gbs": round(gbs, 1)}
             if prec == "fp32":
                 row[prec]["frac_hbm"] = round(gbs / hbm_peak, 4)
+                geo = geo_row(ctx, measure_apply(ctx, torch, prec, flush, reps, pipeline=2), hbm_peak)
+                row["fp32_geo"] = {"ms": round(geo["ms"], 4), "gbs": round(geo["gbs"], 1),
+                                   "frac_hbm": round(geo["frac_hbm"], 4),
+                                   "speedup_vs_stored_factors": round(ms / geo["ms"], 3)}
             else:
                 tf = ctx.n * (16 * ctx.N + 23) / ms / 1e9
                 row[prec]["tflops"] = round(tf, 3)
@@ -934,6 +954,8 @@ def run_ours(args):
                                        "algorithmic_gbs_at_measured_rate": (b32 / (us_per_it * 1e-6) / 1e9)
                                        if us_per_it else None}},
         "apply": ({"fp32_gbs": app["fp32"]["gbs"], "fp32_frac_hbm": app["fp32"]["frac_hbm"],
+                   "fp32_geo_gbs": app["fp32_geo"]["gbs"], "fp32_geo_frac_hbm": app["fp32_geo"]["frac_hbm"],
+                   "fp32_geo_speedup": app["fp32_geo"]["speedup_vs_stored_factors"],
                    "fp64_gbs": app["fp64"]["gbs"], "fp64_tflops": app["fp64"]["tflops"],
                    "fp64_frac_fp64_pipe": app["fp64"]["frac_fp64_pipe"], "fp64_peak_tflops": fp64_peak,
                    "fp64_peak_source": "cuBLAS DGEMM 4096^3 measured in this run",

@@ -104,7 +104,11 @@ enum sem_option {
                                     previous steps exist */
     SEM_OPT_APPLY_PIPELINE = 10  /* FP32 standalone apply: 1 (default) bulk-copy pipelined element
                                     kernel when the input fields are 16-byte aligned, 0 the
-                                    one-pass kernel; same results bit for bit.  A pipelined
+                                    one-pass kernel; same results bit for bit.  2: the pipelined
+                                    kernel computing the geometric factors from each element's
+                                    corners instead of reading them (5 words per node moved
+                                    instead of 9; FP32 rounding of the factors differs from
+                                    the stored ones, within FP32 accuracy).  A pipelined
                                     apply whose bounded wait expired is reported as
                                     SEM_ERR_DEVICE_WAIT by the next sem_dot, solver or
                                     driver call */

@@ -109,6 +109,14 @@ __host__ __device__ constexpr int bulk_arrays()
     return op_nc<OP>() + (OP == OP_MASS ? 0 : 3) + (OP == OP_LAPLACE ? 0 : 1) +
            ((OP == OP_HELM || OP == OP_RES || OP == OP_F) ? 1 : 0);
 }
+// with the geometric factors computed on the fly (GEO, Res only): the two
+// inputs and the potential per node, plus 8 corner differences per element
+template <int OP, bool GEO>
+__host__ __device__ constexpr int bulk_arrays_g()
+{
+    return GEO ? op_nc<OP>() + 1 : bulk_arrays<OP>();
+}
+constexpr int GEO_PER_EL = 8;  // x1-x0, x2-x3, x3-x0, x2-x1, and the same for y
 
 // threads per block: one per element line and component
 template <typename T, int OP>
@@ -143,10 +151,62 @@ __host__ __device__ constexpr int bulk_k(int N)
     return k < q ? q : k;
 }
 
-template <int N, typename T, int OP>
+template <int N, typename T, int OP, bool GEO = false>
 __host__ __device__ constexpr size_t bulk_smem_bytes()
 {
-    return 128 + (size_t)(BULK_STAGES * bulk_arrays<OP>() + 2 * op_nc<OP>()) * bulk_k<T, OP>(N) * N * N * sizeof(T);
+    return 128 + (size_t)(BULK_STAGES * bulk_arrays_g<OP, GEO>() + 2 * op_nc<OP>()) * bulk_k<T, OP>(N) * N * N *
+                     sizeof(T) +
+           (GEO ? (size_t)BULK_STAGES * bulk_k<T, OP>(N) * GEO_PER_EL * sizeof(float) : 0);
+}
+
+// 0.25 (1 - z_i), 0.25 (1 + z_i) and w_i of the LGL nodes, and the metric
+// convention, passed by value (constant-bank operands of the on-the-fly
+// geometric factors)
+template <int N>
+struct GeoTab {
+    float lo[N], hi[N], w[N];
+    int corrected;
+};
+
+// premultiplied factors of node (i, j) from the element's corner differences
+// g (include/Quad.hpp:39-54 as the library's setup evaluates them, in FP32):
+// X_xi, Y_xi at eta_j, X_eta, Y_eta at xi_i, J, and w_i w_j {A, B, C, J}.
+// The thread's own line coordinate (lo, hi, w of its l) comes in registers
+// and the unrolled one from the table, so no index into the table is a
+// runtime value.
+struct GeoLine {
+    float lo, hi, w;
+};
+template <int N>
+__device__ __forceinline__ GeoLine geo_line(const GeoTab<N>& gt, int l)
+{
+    GeoLine r{0.f, 0.f, 0.f};
+#pragma unroll
+    for (int k = 0; k < N; ++k)
+        if (k == l) r = GeoLine{gt.lo[k], gt.hi[k], gt.w[k]};
+    return r;
+}
+// node (i, l): i unrolled, j = l the thread's column line
+template <int N>
+__device__ __forceinline__ void geo_factors_col(const GeoTab<N>& gt, const float* g, int i, const GeoLine& lj,
+                                                float& g11, float& g12, float& g22)
+{
+    const float xxi = lj.lo * g[0] + lj.hi * g[1], yxi = lj.lo * g[4] + lj.hi * g[5];
+    const float xet = gt.lo[i] * g[2] + gt.hi[i] * g[3], yet = gt.lo[i] * g[6] + gt.hi[i] * g[7];
+    const float yx = gt.corrected ? yxi : gt.lo[i] * g[4] + gt.hi[i] * g[5];
+    const float J = xxi * yet - xet * yxi;
+    const float r = (gt.w[i] * lj.w) / J;
+    g11 = (yet * yet + xet * xet) * r;
+    g12 = (yet * yxi + xet * xxi) * r;
+    g22 = (yx * yx + xxi * xxi) * r;
+}
+// w_i w_j J of node (l, j): i = l the thread's row line, j unrolled
+template <int N>
+__device__ __forceinline__ float geo_mass_row(const GeoTab<N>& gt, const float* g, const GeoLine& li, int j)
+{
+    const float xxi = gt.lo[j] * g[0] + gt.hi[j] * g[1], yxi = gt.lo[j] * g[4] + gt.hi[j] * g[5];
+    const float xet = li.lo * g[2] + li.hi * g[3], yet = li.lo * g[6] + li.hi * g[7];
+    return (li.w * gt.w[j]) * (xxi * yet - xet * yxi);
 }
 
 // D(i,k) at [i*N+k], passed by value: the kernel reads it from the constant
@@ -227,15 +287,16 @@ __host__ __device__ constexpr bool bulk_f2(int N) { return N <= 11; }
 // and W2 is written out with one bulk store per component.  Every
 // accumulation runs over k in ascending order as in apply_chunk (the
 // one-pass kernel), so both kernels give the same bits.
-template <int N, typename T, int OP, bool GATHER, bool MG>
+template <int N, typename T, int OP, bool GATHER, bool MG, bool GEO = false>
 __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
     k_apply_bulk(DevMesh m, DMat<N, T> D, DMat2<N> D2, const T* __restrict__ pot, T alpha, const T* __restrict__ in0,
                  const T* __restrict__ in1, T* __restrict__ y0, T* __restrict__ y1, int store_bulk, int pair_asm,
-                 long long timeout_ns)
+                 long long timeout_ns, GeoTab<N> gt)
 {
+    static_assert(!GEO || (OP == OP_RES && MG && sizeof(T) == 4), "on-the-fly geometry: FP32 Res, two components");
     constexpr int NN = N * N;
     constexpr int NC = op_nc<OP>();
-    constexpr int NA = bulk_arrays<OP>();
+    constexpr int NA = bulk_arrays_g<OP, GEO>();
     constexpr int K = bulk_k<T, OP>(N);
     constexpr int BN = K * NN;
     constexpr int S = BULK_STAGES;
@@ -244,22 +305,25 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
     T* stage0 = (T*)(smb + 128);
     T* W1 = stage0 + (size_t)S * NA * BN;
     T* W2 = W1 + NC * BN;
+    float* geo0 = (float*)(W2 + NC * BN);  // GEO: per stage K * GEO_PER_EL corner differences
     const Fac<T> fac = fac_of<T>(m);
     const T* arr[7];
     {
         int a = 0;
         arr[a++] = in0;
         if (NC == 2) arr[a++] = in1;
-        if (OP != OP_MASS) {
-            arr[a++] = fac.g11;
-            arr[a++] = fac.g12;
-            arr[a++] = fac.g22;
+        if (!GEO) {
+            if (OP != OP_MASS) {
+                arr[a++] = fac.g11;
+                arr[a++] = fac.g12;
+                arr[a++] = fac.g22;
+            }
+            if (OP != OP_LAPLACE) arr[a++] = fac.mass;
         }
-        if (OP != OP_LAPLACE) arr[a++] = fac.mass;
         if (OP == OP_HELM || OP == OP_RES || OP == OP_F) arr[a++] = pot;
     }
     T* outp[2] = {y0, y1};
-    constexpr int A_G11 = NC, A_MASS = (OP == OP_MASS) ? NC : NC + 3, A_POT = A_MASS + 1;
+    constexpr int A_G11 = NC, A_MASS = (OP == OP_MASS) ? NC : NC + 3, A_POT = GEO ? NC : A_MASS + 1;
     const long long nfull = m.E / K;  // batches loaded by bulk copies
     const long long nbatch = (m.E + K - 1) / K;
     const long long G = gridDim.x;
@@ -273,9 +337,11 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
         if (b >= nfull) return;
         T* st = stage0 + (size_t)s * NA * BN;
         constexpr uint32_t bytes = (uint32_t)(BN * sizeof(T));
-        mbar_arrive_tx(&bar[s], bytes * NA);
+        constexpr uint32_t gbytes = GEO ? (uint32_t)(K * GEO_PER_EL * sizeof(float)) : 0u;
+        mbar_arrive_tx(&bar[s], bytes * NA + gbytes);
 #pragma unroll
         for (int a = 0; a < NA; ++a) bulk_load(st + a * BN, arr[a] + b * BN, bytes, &bar[s]);
+        if (GEO) bulk_load(geo0 + (size_t)s * K * GEO_PER_EL, m.geo32 + b * K * GEO_PER_EL, gbytes, &bar[s]);
         pending |= 1u << s;
     };
     if (threadIdx.x == 0)
@@ -376,6 +442,9 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
             for (int t = threadIdx.x; t < total; t += blockDim.x)
 #pragma unroll
                 for (int a = 0; a < NA; ++a) st[a * BN + t] = arr[a][(long long)e0 * NN + t];
+            if (GEO)
+                for (int t = threadIdx.x; t < ne * GEO_PER_EL; t += blockDim.x)
+                    geo0[(size_t)s * K * GEO_PER_EL + t] = m.geo32[(long long)e0 * GEO_PER_EL + t];
         }
         if (!__syncthreads_and(ok)) {
             if (threadIdx.x == 0) {
@@ -408,6 +477,8 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
             const bool act = l0 < ne * N;
             const int le = l0 / N, l = l0 - (l0 / N) * N;
             const int base = le * NN;
+            GeoLine gl{};
+            if constexpr (GEO) gl = geo_line<N>(gt, l);
             T* w1a = W1 + base;
             T* w1b = W1 + BN + base;
             T* w2a = W2 + base;
@@ -446,10 +517,22 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
             // ---- P2: column l: fluxes (factors read once); f2 -> W1, lap1 = D^T f1 -> W2
             if (act) {
                 T fa[N], fb[N], aa[N], ab[N];
+                float gq[GEO_PER_EL];
+                if (GEO) {
+#pragma unroll
+                    for (int k = 0; k < GEO_PER_EL; ++k) gq[k] = geo0[((size_t)s * K + le) * GEO_PER_EL + k];
+                }
 #pragma unroll
                 for (int i = 0; i < N; ++i) {
                     const int q = base + l * N + i;
-                    const T g11 = st[A_G11 * BN + q], g12 = st[(A_G11 + 1) * BN + q], g22 = st[(A_G11 + 2) * BN + q];
+                    T g11, g12, g22;
+                    if constexpr (GEO) {
+                        geo_factors_col<N>(gt, gq, i, gl, g11, g12, g22);
+                    } else {
+                        g11 = st[A_G11 * BN + q];
+                        g12 = st[(A_G11 + 1) * BN + q];
+                        g22 = st[(A_G11 + 2) * BN + q];
+                    }
                     const T usa = w1a[l * N + i], usb = w1b[l * N + i];
                     fa[i] = g11 * ura[i] - g12 * usa;
                     fb[i] = g11 * urb[i] - g12 * usb;
@@ -479,10 +562,20 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
                     fb[j] = w1b[j * N + l];
                 }
                 contract2<N, true, bulk_f2(N)>(D, D2, fa, fb, la, lb);
+                float gq[GEO_PER_EL];
+                if (GEO) {
+#pragma unroll
+                    for (int k = 0; k < GEO_PER_EL; ++k) gq[k] = geo0[((size_t)s * K + le) * GEO_PER_EL + k];
+                }
 #pragma unroll
                 for (int j = 0; j < N; ++j) {
                     const int q = base + j * N + l;
-                    const T ms = st[A_MASS * BN + q];
+                    T ms;
+                    if constexpr (GEO) {
+                        ms = geo_mass_row<N>(gt, gq, gl, j);
+                    } else {
+                        ms = st[A_MASS * BN + q];
+                    }
                     const T pv = st[A_POT * BN + q];
                     const T mv = ms * pv;
                     const T u0 = st[q], u1 = st[BN + q];
@@ -660,7 +753,7 @@ __global__ void __launch_bounds__(bulk_tpb_k<T, OP, MG>())
 // grid of k_apply_bulk for one instantiation.  The shared-memory opt-in is
 // a per-device attribute, so it is set, and the occupancy queried, once per
 // device (the current one, which owns the launch's stream), under a lock.
-template <int N, typename T, int OP, bool GATHER, bool MG>
+template <int N, typename T, int OP, bool GATHER, bool MG, bool GEO>
 cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
                                  bool pair_asm, long long timeout_ns, cudaStream_t st)
 {
@@ -668,8 +761,9 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     static std::mutex mu;
     static bool ready[kMaxDev] = {};
     static int blocks_per_sm_of[kMaxDev] = {}, sms_of[kMaxDev] = {};
-    constexpr size_t smem = bulk_smem_bytes<N, T, OP>();
+    constexpr size_t smem = bulk_smem_bytes<N, T, OP, GEO>();
     constexpr int TPB = bulk_tpb_k<T, OP, MG>();
+    const auto kern = k_apply_bulk<N, T, OP, GATHER, MG, GEO>;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -678,13 +772,11 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     {
         std::lock_guard<std::mutex> lk(mu);
         if (!ready[dev]) {
-            e = cudaFuncSetAttribute(k_apply_bulk<N, T, OP, GATHER, MG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+            e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
             if (e != cudaSuccess) return e;
             if ((e = cudaDeviceGetAttribute(&sms_of[dev], cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
                 return e;
-            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm_of[dev],
-                                                                   k_apply_bulk<N, T, OP, GATHER, MG>, TPB, smem)) !=
+            if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm_of[dev], kern, TPB, smem)) !=
                 cudaSuccess)
                 return e;
             ready[dev] = true;
@@ -694,6 +786,7 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     }
     if (blocks_per_sm < 1) return cudaErrorInvalidConfiguration;
     if (!m.Dh) return cudaErrorInvalidValue;
+    if (GEO && (!m.geo32 || !m.zh || !m.wh)) return cudaErrorInvalidValue;
     DMat<N, T> D;
     DMat2<N> D2 = {};
     for (int i = 0; i < N * N; ++i) {
@@ -705,6 +798,15 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
             D2.d[i] = ((unsigned long long)u << 32) | u;
         }
     }
+    GeoTab<N> gt = {};
+    if (GEO) {
+        for (int i = 0; i < N; ++i) {
+            gt.lo[i] = (float)(0.25 * (1.0 - m.zh[i]));
+            gt.hi[i] = (float)(0.25 * (1.0 + m.zh[i]));
+            gt.w[i] = (float)m.wh[i];
+        }
+        gt.corrected = m.corrected;
+    }
     constexpr int K = bulk_k<T, OP>(N);
     const long long nbatch = (m.E + K - 1) / K;
     const int grid = (int)std::min<long long>(nbatch, (long long)sms * blocks_per_sm);
@@ -712,8 +814,7 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
     // batch-local pair tables exist for the FP32 Res batching only
     const int pa = (pair_asm && OP == OP_RES && sizeof(T) == 4 && m.bulk_K == K && m.bulk_pair_ptr) ? 1 : 0;
     if (pair_asm && !pa) return cudaErrorInvalidValue;
-    k_apply_bulk<N, T, OP, GATHER, MG>
-        <<<grid, TPB, smem, st>>>(m, D, D2, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns);
+    kern<<<grid, TPB, smem, st>>>(m, D, D2, pot, alpha, in0, in1, y0, y1, store_bulk, pa, timeout_ns, gt);
     return cudaGetLastError();
 }
 
@@ -723,12 +824,20 @@ cudaError_t launch_apply_bulk_mg(const DevMesh& m, const T* pot, T alpha, const 
 // elements and most of its threads have no line
 __host__ __device__ constexpr bool bulk_mg(int N) { return !(N == 13 || N == 14 || N == 17); }
 
+// geo: the geometric factors computed on the fly from the element corners
+// (FP32 Res with both components per thread); otherwise they are read
 template <int N, typename T, int OP, bool GATHER>
 cudaError_t launch_apply_bulk_t(const DevMesh& m, const T* pot, T alpha, const T* in0, const T* in1, T* y0, T* y1,
-                                bool pair_asm, long long timeout_ns, cudaStream_t st)
+                                bool pair_asm, bool geo, long long timeout_ns, cudaStream_t st)
 {
     constexpr bool MG = OP == OP_RES && bulk_mg(N);
-    return launch_apply_bulk_mg<N, T, OP, GATHER, MG>(m, pot, alpha, in0, in1, y0, y1, pair_asm, timeout_ns, st);
+    if constexpr (MG && sizeof(T) == 4) {
+        if (geo)
+            return launch_apply_bulk_mg<N, T, OP, GATHER, MG, true>(m, pot, alpha, in0, in1, y0, y1, pair_asm,
+                                                                    timeout_ns, st);
+    }
+    return launch_apply_bulk_mg<N, T, OP, GATHER, MG, false>(m, pot, alpha, in0, in1, y0, y1, pair_asm, timeout_ns,
+                                                             st);
 }
 
 }  // namespace semgb

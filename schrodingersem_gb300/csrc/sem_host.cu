@@ -675,6 +675,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
     c->B.assign(c->n, 0.0);
     c->C.assign(c->n, 0.0);
     std::vector<double> g11(c->n), g12(c->n), g22(c->n), ms(c->n);
+    std::vector<float> geo((size_t)n_el * 8);  // corner differences of the on-the-fly FP32 apply
     const std::vector<double>& z = c->x;
     for (int e = 0; e < n_el; ++e) {
         double xs[4], ys[4];
@@ -682,6 +683,9 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
             xs[k] = coords[2 * elements[4 * e + k]];
             ys[k] = coords[2 * elements[4 * e + k] + 1];
         }
+        const double gd[8] = {xs[1] - xs[0], xs[2] - xs[3], xs[3] - xs[0], xs[2] - xs[1],
+                              ys[1] - ys[0], ys[2] - ys[3], ys[3] - ys[0], ys[2] - ys[1]};
+        for (int k = 0; k < 8; ++k) geo[(size_t)e * 8 + k] = (float)gd[k];
         double Xxi[MAX_N], Yxi[MAX_N], Xeta[MAX_N], Yeta[MAX_N];
         for (int i = 0; i < N; ++i) {
             Xxi[i] = 0.25 * ((1 - z[i]) * (xs[1] - xs[0]) + (1 + z[i]) * (xs[2] - xs[3]));
@@ -779,6 +783,9 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         }
     c->Drow_host = Drow;
     d.Dh = c->Drow_host.data();
+    d.zh = c->x.data();
+    d.wh = c->w.data();
+    d.corrected = corrected ? 1 : 0;
     auto tof = [](const std::vector<double>& v) {
         std::vector<float> f(v.size());
         for (size_t i = 0; i < v.size(); ++i) f[i] = (float)v[i];
@@ -803,7 +810,8 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
         (s = upload(c, node_nb, &d.node_nb)) ||
         (s = upload(c, bulk_pair_ptr, &d.bulk_pair_ptr)) ||
         (!bulk_pairs.empty() && (s = upload(c, bulk_pairs, &d.bulk_pairs))) ||
-        (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)))
+        (s = upload(c, bnd_flat, &d.bnd_flat)) || (s = upload(c, node_bnd, &d.node_bnd)) ||
+        (s = upload(c, geo, &d.geo32)))
         return s;
     d.n_pairs = (long long)edge_pairs.size();
     d.n_pairs_x = n_pairs_x;
@@ -966,7 +974,7 @@ extern "C" int sem_ctx_set_option(sem_ctx* c, int opt, double v)
             c->extrap_order = (int)v;
             return SEM_OK;
         case SEM_OPT_APPLY_PIPELINE:
-            if (v != 0 && v != 1) return fail(SEM_ERR_ARG, "apply pipeline must be 0 or 1");
+            if (v != 0 && v != 1 && v != 2) return fail(SEM_ERR_ARG, "apply pipeline must be 0, 1 or 2");
             c->apply_pipeline = (int)v;
             return SEM_OK;
         case SEM_OPT_LEARNED_STEP:
@@ -1257,7 +1265,8 @@ extern "C" int sem_apply_schro_res_f32(sem_ctx* c, const float* V, float alpha, 
         if (bulk) {
             SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
                 return launch_apply_bulk<decltype(nv)::value>(c->dm, OP_RES, true, V, alpha, qr, qi, yr, yi, true,
-                                                              true, timeout_ns(c), c->stream);
+                                                              true, c->apply_pipeline == 2, timeout_ns(c),
+                                                              c->stream);
             }));
         } else {
             SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
@@ -1879,8 +1888,10 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     if ((s = wsget(c, "lr_delta", (size_t)c->E * 2 * NN, &delta)) || (s = wsget(c, "lr_zl", 2 * c->n, &zl)) ||
         (s = wsget(c, "lr_r2", 2 * c->n, &r2)))
         return s;
+    const long long fl0 = learner_forward_launches(c->learner);
     if ((s = sem_learner_set_stream(c->learner, c->stream)) || (s = sem_learner_forward(c->learner, c->E, x, delta)))
         return s;
+    c->stats.kernel_launches += learner_forward_launches(c->learner) - fl0;
     LearnArgs k{};
     k.what = LEARN_CORRECT;
     k.zg = zx;

@@ -96,6 +96,13 @@ struct DevMesh {
     const int* bulk_pairs = nullptr;
     int* dev_err = nullptr;  // set by a kernel whose bounded wait expired (pipelined apply)
     const double* Dh = nullptr;  // host copy of D, row-major (launchers that pass D by value)
+    // on-the-fly geometry of the FP32 Res apply: per element {x1-x0, x2-x3,
+    // x3-x0, x2-x1, y1-y0, y2-y3, y3-y0, y2-y1} (FP32), the host LGL nodes and
+    // weights, and the metric convention (1: SEM_FLAG_METRIC_CORRECTED)
+    const float* geo32 = nullptr;
+    const double* zh = nullptr;
+    const double* wh = nullptr;
+    int corrected = 0;
 };
 
 // Grid barrier and error state of a persistent (cooperative) kernel.
@@ -172,10 +179,12 @@ cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, d
 // field pointer 16-byte aligned (FP64 applies are FP64-pipe bound and use
 // the one-pass kernel).  pair_asm: the kernel also sums the side pairs inside
 // its batches (the masked output then needs launch_ring with cross_only).
+// geo: the geometric factors computed on the fly from the element corners
+// (FP32 Res; DevMesh::geo32), not read from the stored planes
 template <int N>
 cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
-                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, long long timeout_ns,
-                              cudaStream_t st);
+                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, bool geo,
+                              long long timeout_ns, cudaStream_t st);
 template <int N>
 cudaError_t launch_dss(const DevMesh& m, bool fp32, int mode, double scale, const void* y,
                        void* out, cudaStream_t st);
@@ -270,6 +279,9 @@ int ctx_device(const sem_ctx* c);     // ordinal of the device the context was c
 void ctx_count_fp64_apply(sem_ctx* c);  // one more FP64 operator apply in sem_stats
 int ctx_fail(int code, const char* msg);  // records the message, returns code
 }  // namespace semgb
+// kernels launched by a network's forward passes so far (defined in sem_mlp.cu)
+struct sem_learner;
+long long learner_forward_launches(const sem_learner* L);
 
 #define SEM_FOR_EACH_N(X) \
     X(2) X(3) X(4) X(5) X(6) X(7) X(8) X(9) X(10) X(11) X(12) X(13) X(14) X(15) X(16) X(17)

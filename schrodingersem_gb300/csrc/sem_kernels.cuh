@@ -414,16 +414,16 @@ cudaError_t launch_apply(const DevMesh& m, int op, bool fp32, const void* pot, d
 
 template <int N>
 cudaError_t launch_apply_bulk(const DevMesh& m, int op, bool fp32, const void* pot, double alpha, const void* in0,
-                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, long long timeout_ns,
-                              cudaStream_t st)
+                              const void* in1, void* y0, void* y1, bool gather, bool pair_asm, bool geo,
+                              long long timeout_ns, cudaStream_t st)
 {
 #define SEM_BULK_CASE(T, OPK)                                                                                 \
     return gather ? launch_apply_bulk_t<N, T, OPK, true>(m, (const T*)pot, (T)alpha, (const T*)in0,           \
-                                                         (const T*)in1, (T*)y0, (T*)y1, pair_asm, timeout_ns, \
-                                                         st)                                                  \
+                                                         (const T*)in1, (T*)y0, (T*)y1, pair_asm, geo,        \
+                                                         timeout_ns, st)                                      \
                   : launch_apply_bulk_t<N, T, OPK, false>(m, (const T*)pot, (T)alpha, (const T*)in0,          \
-                                                          (const T*)in1, (T*)y0, (T*)y1, pair_asm, timeout_ns, \
-                                                          st);
+                                                          (const T*)in1, (T*)y0, (T*)y1, pair_asm, geo,       \
+                                                          timeout_ns, st);
     if (!fp32) return cudaErrorInvalidValue;  // FP64 applies are FP64-pipe bound: one-pass kernel
     switch (op) {
         case OP_RES: SEM_BULK_CASE(float, OP_RES)
@@ -593,7 +593,7 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
     template cudaError_t launch_ring<NV>(const DevMesh&, bool, int, void*, void*, bool, cudaStream_t); \
     template cudaError_t launch_apply_bulk<NV>(const DevMesh&, int, bool, const void*, double,       \
                                                const void*, const void*, void*, void*, bool, bool,   \
-                                               long long, cudaStream_t);                             \
+                                               bool, long long, cudaStream_t);                       \
     template cudaError_t launch_unmask<NV>(const DevMesh&, bool, void*, cudaStream_t);               \
     template cudaError_t launch_mask<NV>(const DevMesh&, bool, void*, cudaStream_t);                 \
     template cudaError_t launch_dot<NV>(const DevMesh&, const double*, const double*, double*, int,  \

@@ -470,6 +470,7 @@ struct sem_learner {
     __nv_bfloat16 *h1bf = nullptr, *h2bf = nullptr;
     double* loss = nullptr;
     long long adam_t = 0;
+    long long forward_launches = 0;  // kernels launched by forward passes
     cudaStream_t stream = nullptr;
     std::string err;
     int din(int l) const { return l == 0 ? d_in : H; }
@@ -626,6 +627,7 @@ static int forward(sem_learner* L, int rows, const __nv_bfloat16* x)
         }
         LCUDA(cudaGetLastError());
         L->wt_dirty = false;
+        L->forward_launches += 3;
     }
     // B(k, n) = W[k][n] = WT[n][k]: K contiguous
     GemmArgs g{};
@@ -640,8 +642,11 @@ static int forward(sem_learner* L, int rows, const __nv_bfloat16* x)
     g.N = L->d_out; g.A = L->h2bf; g.B = L->WbfT[2]; g.sb_n = L->H;
     g.C = L->out; g.ldc = L->d_out; g.bias = L->b[2]; g.relu = 0; g.Cbf = nullptr;
     LCUDA(gemm(g, L->stream));
+    L->forward_launches += 3;
     return SEM_OK;
 }
+
+long long learner_forward_launches(const sem_learner* L) { return L ? L->forward_launches : 0; }
 
 // predictions for rows x d_in BF16 inputs into out (device FP32, rows x d_out)
 extern "C" int sem_learner_forward(sem_learner* L, int rows, const void* x_bf16, float* out)

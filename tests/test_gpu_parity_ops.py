@@ -186,6 +186,7 @@ def test_pipelined_apply_matches_one_pass_kernel(semlib, oracle, n, p, order):
     f = torch.float32
 
     def run_all():
+        ctx.set_option(capi.OPT_APPLY_PIPELINE, 1)
         out = [ctx.apply_laplace(u), ctx.apply_helmholtz(V, u), ctx.gproj(u)]
         out += list(ctx.schro_res(V, 0.02, u, v)) + list(ctx.schro_f(V, u, v))
         out += list(ctx.schro_res_f32(V.to(f), 0.02, u.to(f), v.to(f)))
@@ -194,9 +195,61 @@ def test_pipelined_apply_matches_one_pass_kernel(semlib, oracle, n, p, order):
 
     a = run_all()
     ctx.set_option(capi.OPT_APPLY_PIPELINE, 0)
-    b = run_all()
+    b = [ctx.apply_laplace(u), ctx.apply_helmholtz(V, u), ctx.gproj(u)]
+    b += list(ctx.schro_res(V, 0.02, u, v)) + list(ctx.schro_f(V, u, v))
+    b += list(ctx.schro_res_f32(V.to(f), 0.02, u.to(f), v.to(f)))
+    torch.cuda.synchronize()
     for x, y in zip(a, b):
         assert torch.equal(x, y)
     if n <= 7:
         om = oracle.Mesh(p, coords=co, elements=el)
         assert rel_err(a[0].cpu().numpy(), om.apply_laplace(u.cpu().numpy())) <= TOL64
+
+
+@pytest.mark.parametrize("n,p,order,corrected,neumann", [
+    (5, 1, "rows", False, False), (24, 8, "rows", False, False), (24, 8, "shuffled", True, False),
+    (9, 3, "shuffled", False, True), (12, 4, "rows", True, True), (7, 12, "rows", False, False),
+    (6, 15, "shuffled", True, False), (40, 6, "rows", False, False)])
+def test_on_the_fly_geometry_apply_fp32(semlib, oracle, n, p, order, corrected, neumann):
+    """FP32 Res apply with the geometric factors computed inside the
+    pipelined kernel from each element's corner differences (apply pipeline
+    2): within the FP32 tolerance of the oracle's FP64 Res (include/Quad.hpp:39-54
+    metrics, both metric conventions, Dirichlet and natural boundaries,
+    shuffled and rotated elements, mesh tails), and close to the pipelined
+    kernel that reads the stored FP32 factors"""
+    import torch
+    from schrodingersem_gb300 import capi
+    co, el = structured(n, box=(-1.0, 2.0, -0.5, 1.5), jitter=0.2, seed=3 * n + p)
+    if order == "shuffled":
+        rng = np.random.default_rng(11 * n + p)
+        el = el[rng.permutation(len(el))]
+        el = np.stack([np.roll(row, int(r)) for row, r in zip(el, rng.integers(0, 4, len(el)))])
+    ctx = semlib.Context(p, coords=co, elements=el, corrected_metric=corrected, neumann=neumann)
+    om = oracle.Mesh(p, coords=co, elements=el, ref_compat=not corrected, neumann=neumann)
+    rng = np.random.default_rng(70 + p)
+    u, v = rng.standard_normal(om.shape), rng.standard_normal(om.shape)
+    V = rng.uniform(-5, 5, om.shape)
+    f = torch.float32
+    args = (ctx.to_device(V, f), 0.04, ctx.to_device(u, f), ctx.to_device(v, f))
+    ctx.set_option(capi.OPT_APPLY_PIPELINE, 2)
+    gr, gi = ctx.schro_res_f32(*args)
+    ctx.set_option(capi.OPT_APPLY_PIPELINE, 1)
+    sr, si = ctx.schro_res_f32(*args)
+    torch.cuda.synchronize()
+    c32 = lambda a: a.astype(np.float32).astype(np.float64)  # noqa: E731
+    orr, oii = om.schro_res(c32(V), 0.04, c32(u), c32(v))
+    assert rel_err(gr.cpu().double().numpy(), orr) <= TOL32
+    assert rel_err(gi.cpu().double().numpy(), oii) <= TOL32
+    assert rel_err(gr.cpu().double().numpy(), sr.cpu().double().numpy()) <= TOL32
+    assert rel_err(gi.cpu().double().numpy(), si.cpu().double().numpy()) <= TOL32
+    ctx.dot(ctx.to_device(u), ctx.to_device(v))  # raises if a bounded wait of the kernel expired
+
+
+def test_apply_pipeline_option_range(semlib):
+    from schrodingersem_gb300 import capi
+    co, el = structured(4, box=(0.0, 1.0, 0.0, 1.0), jitter=0.1, seed=1)
+    ctx = semlib.Context(4, coords=co, elements=el)
+    for v in (0, 1, 2):
+        ctx.set_option(capi.OPT_APPLY_PIPELINE, v)
+    with pytest.raises(capi.SemError):
+        ctx.set_option(capi.OPT_APPLY_PIPELINE, 3)
