@@ -84,26 +84,34 @@ __device__ __forceinline__ unsigned long long res_ld(const unsigned long long* p
 // eta lines (c, le, i): stride N from base = c*st + le*N^2 + i.  Line L is
 // (c, pos, le) with the element fastest.  Lines of one pass are disjoint, so
 // each pass may write in place.
+// element count of the block and its FP32 reciprocal: (rem + 0.5) * (1/ne)
+// in FP32 is at least 0.5 / ne from an integer and within a few ulp of the
+// exact quotient, so its truncation is rem / ne (checked exhaustively for
+// ne <= 1024, rem < 34 ne)
+struct ResNe {
+    int n;
+    float inv;
+};
 template <int N>
-__device__ __forceinline__ void res_line(int L, int ne, int st, bool xi, int& base, int& fb, int& pos)
+__device__ __forceinline__ void res_line(int L, ResNe ne, int st, bool xi, int& base, int& fb, int& pos)
 {
     constexpr int NN = N * N;
-    const int per = ne * N;
+    const int per = ne.n * N;
     const int c = L >= per ? 1 : 0;
     const int rem = L - c * per;
-    pos = rem / ne;  // j of a xi line, i of an eta line
+    pos = (int)(((float)rem + 0.5f) * ne.inv);  // rem / ne: j of a xi line, i of an eta line
     // consecutive threads take the same line of consecutive elements: with an
     // odd N the element stride N^2 spreads a warp over all 32 banks
-    const int le = rem - pos * ne;
+    const int le = rem - pos * ne.n;
     fb = le * NN + (xi ? pos * N : pos);
     base = c * st + fb;
 }
 
 // apply pass X1: A = D u along xi (u_xi)
 template <int N>
-__device__ __forceinline__ void res_apply_x1(const ResCoef<N>& cf, const float* U, float* A, int ne, int st)
+__device__ __forceinline__ void res_apply_x1(const ResCoef<N>& cf, const float* U, float* A, ResNe ne, int st)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, true, base, fb, pos);
         float u[N];
@@ -123,9 +131,9 @@ __device__ __forceinline__ void res_apply_x1(const ResCoef<N>& cf, const float* 
 // f1 = g11 u_xi - g12 u_eta (into A) and f2 = g22 u_eta - g12 u_xi (into B)
 template <int N>
 __device__ __forceinline__ void res_apply_y1(const ResCoef<N>& cf, const float* U, float* A, float* B,
-                                             const float* G11, const float* G12, const float* G22, int ne, int st)
+                                             const float* G11, const float* G12, const float* G22, ResNe ne, int st)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, false, base, fb, pos);
         float u[N], ur[N];
@@ -148,9 +156,9 @@ __device__ __forceinline__ void res_apply_y1(const ResCoef<N>& cf, const float* 
 
 // apply pass X2: A = D^T f1 along xi (first half of the weak divergence)
 template <int N>
-__device__ __forceinline__ void res_apply_x2(const ResCoef<N>& cf, float* A, int ne, int st)
+__device__ __forceinline__ void res_apply_x2(const ResCoef<N>& cf, float* A, ResNe ne, int st)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, true, base, fb, pos);
         float f[N];
@@ -168,9 +176,9 @@ __device__ __forceinline__ void res_apply_x2(const ResCoef<N>& cf, float* A, int
 
 // apply pass Y2: A += D^T f2 along eta (continuing the same FMA chain)
 template <int N>
-__device__ __forceinline__ void res_apply_y2(const ResCoef<N>& cf, float* A, const float* B, int ne, int st)
+__device__ __forceinline__ void res_apply_y2(const ResCoef<N>& cf, float* A, const float* B, ResNe ne, int st)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, false, base, fb, pos);
         float f[N], a1[N];
@@ -194,9 +202,9 @@ __device__ __forceinline__ void res_apply_y2(const ResCoef<N>& cf, float* A, con
 // F4 z = t S^T along eta, times the Neumann-Neumann weight, ring copies to Xout
 // (tagged words, see res_exchange)
 template <int N>
-__device__ __forceinline__ void res_fdm_xi(const ResCoef<N>& cf, float* B, int ne, int st, bool transpose)
+__device__ __forceinline__ void res_fdm_xi(const ResCoef<N>& cf, float* B, ResNe ne, int st, bool transpose)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, true, base, fb, pos);
         float u[N];
@@ -213,9 +221,9 @@ __device__ __forceinline__ void res_fdm_xi(const ResCoef<N>& cf, float* B, int n
 }
 
 template <int N>
-__device__ __forceinline__ void res_fdm_f2(const ResCoef<N>& cf, float* B, const float* FD, int ne, int st)
+__device__ __forceinline__ void res_fdm_f2(const ResCoef<N>& cf, float* B, const float* FD, ResNe ne, int st)
 {
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, false, base, fb, pos);
         float t[N];
@@ -233,10 +241,10 @@ __device__ __forceinline__ void res_fdm_f2(const ResCoef<N>& cf, float* B, const
 
 template <int N>
 __device__ __forceinline__ void res_fdm_f4(const ResCoef<N>& cf, float* B, const float* WT, unsigned long long* Xout,
-                                           unsigned tag, int ne, int st, long long n, int eb)
+                                           unsigned tag, ResNe ne, int st, long long n, int eb)
 {
     constexpr int NN = N * N;
-    for (int L = threadIdx.x; L < 2 * ne * N; L += RES_TPB) {
+    for (int L = threadIdx.x; L < 2 * ne.n * N; L += RES_TPB) {
         int base, fb, pos;
         res_line<N>(L, ne, st, false, base, fb, pos);
         const int c = base >= st ? 1 : 0;
@@ -514,14 +522,15 @@ __device__ __forceinline__ void res_apply(const ResCoef<N>& cf, float* sm, int s
     float* U = sm + 8 * st;
     float* A = sm + 10 * st;
     float* B = sm + 12 * st;
+    const ResNe nb{ne, 1.f / (float)ne};
     __syncthreads();
-    res_apply_x1<N>(cf, U, A, ne, st);
+    res_apply_x1<N>(cf, U, A, nb, st);
     __syncthreads();
-    res_apply_y1<N>(cf, U, A, B, sm, sm + st, sm + 2 * st, ne, st);
+    res_apply_y1<N>(cf, U, A, B, sm, sm + st, sm + 2 * st, nb, st);
     __syncthreads();
-    res_apply_x2<N>(cf, A, ne, st);
+    res_apply_x2<N>(cf, A, nb, st);
     __syncthreads();
-    res_apply_y2<N>(cf, A, B, ne, st);
+    res_apply_y2<N>(cf, A, B, nb, st);
     __syncthreads();
     res_combine<N>(U, A, sm + 3 * st, sm + 4 * st, X, tag, st, eb, ne * N * N, alpha, n);
 }
@@ -531,14 +540,15 @@ __device__ __forceinline__ void res_precond(const ResCoef<N>& cf, float* sm, int
                                             unsigned long long* X, unsigned tag, long long n)
 {
     float* B = sm + 12 * st;
+    const ResNe nb{ne, 1.f / (float)ne};
     __syncthreads();
-    res_fdm_xi<N>(cf, B, ne, st, true);
+    res_fdm_xi<N>(cf, B, nb, st, true);
     __syncthreads();
-    res_fdm_f2<N>(cf, B, sm + 5 * st, ne, st);
+    res_fdm_f2<N>(cf, B, sm + 5 * st, nb, st);
     __syncthreads();
-    res_fdm_xi<N>(cf, B, ne, st, false);
+    res_fdm_xi<N>(cf, B, nb, st, false);
     __syncthreads();
-    res_fdm_f4<N>(cf, B, sm + 6 * st, X, tag, ne, st, n, eb);
+    res_fdm_f4<N>(cf, B, sm + 6 * st, X, tag, nb, st, n, eb);
 }
 
 struct ResOut {
