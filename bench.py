@@ -60,7 +60,7 @@ ORACLE_TOL = 1e-13  # MINRES tolerance of the FP64 accuracy reference runs
 # capture summarised in profiles/k_minres_resident_64x64_p8.md (mean of three
 # launches).  The Krylov vectors stay on chip; these bytes are the FP64
 # refinement's fields and the per-launch loads.
-SOLVER_DRAM_BYTES_PER_LAUNCH = 41.24e6
+SOLVER_DRAM_BYTES_PER_LAUNCH = 40.94e6
 APPLY_NEL = 559  # 559^2 elements at p = 8: 4473^2 = 20.0 M global nodes
 
 
