@@ -144,6 +144,61 @@ __global__ void k_lincomb_n(long long n, PtrList L, double* __restrict__ out)
     }
 }
 
+// Step length of the learned guess from launch_dot3's partials of
+// (r_ext.r_ext, r_ext.r_l, r_l.r_l), summed in a fixed order: the step theta
+// along d = z_l - z_ext minimising |r_ext - theta A d| (A d = r_ext - r_l),
+// or the whole step when full_step and the prediction is finite and raises
+// the residual at most tenfold.  st = (|r_ext|^2, theta, residual ratio,
+// accepted 1/0).
+__global__ void __launch_bounds__(256) k_learn_theta(const double* __restrict__ part, int used, int full_step,
+                                                     double* __restrict__ st)
+{
+    __shared__ double red[3][256];
+    double a = 0.0, b = 0.0, c = 0.0;
+    for (int i = threadIdx.x; i < used; i += 256) {
+        a += part[3 * i];
+        b += part[3 * i + 1];
+        c += part[3 * i + 2];
+    }
+    red[0][threadIdx.x] = a;
+    red[1][threadIdx.x] = b;
+    red[2][threadIdx.x] = c;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w)
+#pragma unroll
+            for (int q = 0; q < 3; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double n_ext = red[0][0], rx = red[1][0], n_l = red[2][0];
+        const double den = n_ext - 2.0 * rx + n_l;
+        double theta = den > 0 ? (n_ext - rx) / den : 0.0;
+        if (full_step && isfinite(n_l) && n_l <= 100.0 * n_ext) theta = 1.0;
+        double ratio = 1.0, acc = 0.0;
+        if (theta > 0 && n_ext > 0) {
+            acc = 1.0;
+            const double n_t = n_ext - 2.0 * theta * (n_ext - rx) + theta * theta * den;  // |r_ext - theta A d|^2
+            ratio = sqrt(fmax(0.0, n_t) / n_ext);
+        }
+        st[0] = n_ext;
+        st[1] = theta;
+        st[2] = ratio;
+        st[3] = acc;
+    }
+}
+
+// z = (1 - theta) z_ext + theta z_l when the step was accepted (st[3]);
+// otherwise z keeps the base guess
+__global__ void k_learn_step(long long n, const double* __restrict__ zx, const double* __restrict__ zl,
+                             const double* __restrict__ st, double* __restrict__ z)
+{
+    if (st[3] == 0.0) return;
+    const double th = st[1];
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        z[i] = (1.0 - th) * zx[i] + th * zl[i];
+}
+
 static int grid_1d(long long n) { return (int)std::min<long long>((n + 255) / 256, 152 * 16); }
 
 // dynamic shared memory a persistent solver block may use for staging
@@ -297,6 +352,9 @@ struct sem_ctx {
     int apply_pipeline = 1;
     int extrap_order = 1;
     int learned_step = 0;  // SEM_OPT_LEARNED_STEP
+    // |r|^2 of the last learned guess's base residual: the feature scale
+    // floor of the next guess (saves a read-back per stage); < 0 unknown
+    double lr_nrm2 = -1.0;
     int adaptive_inner = 1;
     int resident = 1;
     // projection stage guess: basis size (0 off), slots in use, next slot,
@@ -318,6 +376,8 @@ struct sem_ctx {
     std::unordered_map<std::string, DevBuf> ws;
     SolveOut* h_out = nullptr;  // pinned
     GridSync* h_sync = nullptr; // pinned
+    double* h_lstat = nullptr;  // pinned: the last learned step's (|r|^2, theta, ratio, accepted)
+    bool lr_pending = false;    // h_lstat holds a step whose statistics are not collected yet
     double* h_part = nullptr;   // pinned partials for dots
 };
 
@@ -826,6 +886,7 @@ static int build_ctx(sem_ctx* c, int p, int n_nodes, const double* coords, int n
     SEM_CUDA(cudaMallocHost((void**)&c->h_out, sizeof(SolveOut)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_sync, sizeof(GridSync)));
     SEM_CUDA(cudaMallocHost((void**)&c->h_part, sizeof(double) * 152 * 64));
+    SEM_CUDA(cudaMallocHost((void**)&c->h_lstat, sizeof(double) * 4));
     return SEM_OK;
 }
 
@@ -904,6 +965,7 @@ extern "C" int sem_ctx_destroy(sem_ctx* c)
         if (kv.second.p) cudaFree(kv.second.p);
     if (c->h_out) cudaFreeHost(c->h_out);
     if (c->h_sync) cudaFreeHost(c->h_sync);
+    if (c->h_lstat) cudaFreeHost(c->h_lstat);
     if (c->h_part) cudaFreeHost(c->h_part);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
@@ -1870,14 +1932,20 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
         SEM_CUDA(cudaMemcpyAsync(r, rbase, sizeof(double) * 2 * c->n, cudaMemcpyDeviceToDevice, c->stream));
     else if ((s = guess_residual(c, V, alpha, b, zx, r)))
         return s;
-    double n_ext = 0;
-    if ((s = dots3(c, r, r, &n_ext, nullptr, nullptr))) return s;
+    // per-element scale floor: 1e-6 of the residual's RMS over all copies.
+    // A prediction takes |r|^2 from the previous learned guess of the run
+    // (the floor only keeps round-off out of the features); the first one,
+    // and every training sample, reads it back for this residual
+    double n_ext = c->lr_nrm2;
+    if (!use || !(n_ext > 0)) {
+        if ((s = dots3(c, r, r, &n_ext, nullptr, nullptr))) return s;
+        c->lr_nrm2 = n_ext;
+    }
     LearnArgs a{};
     a.what = LEARN_FEATURES;
     a.r = r;
     a.V = V;
     a.alpha = alpha;
-    // per-element scale floor: 1e-6 of the residual's RMS over all copies
     a.rho_floor = std::max(1e-6 * std::sqrt(n_ext / (2.0 * (double)c->n)), 1e-300);
     a.x = x;
     a.sigma = sig;
@@ -1902,27 +1970,40 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     if ((s = guess_residual(c, V, alpha, b, zl, r2))) return s;
     // minimal residual along the predicted correction d = z_l - z_ext:
     // r(theta) = r_ext - theta A d with A d = r_ext - r_l, so
-    // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|
-    double n_l = 0, rx = 0;
-    if ((s = dots3(c, r, r2, nullptr, &rx, &n_l))) return s;
-    const double den = n_ext - 2.0 * rx + n_l;
-    double theta = den > 0 ? (n_ext - rx) / den : 0.0;
-    // full step: the prediction as it is, unless it is not finite or raises
-    // the residual more than tenfold (then the residual-minimising step)
-    if (c->learned_step == 1 && std::isfinite(n_l) && n_l <= 100.0 * n_ext) theta = 1.0;
+    // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|.
+    // The step is taken on the device (no read-back before the solve); its
+    // statistics are collected after the stage solve (learned_collect)
+    double* part = nullptr;
+    double* dst = nullptr;
+    if ((s = wsget(c, "dot_part", 152 * 64, &part)) || (s = wsget(c, "lr_stat", 4, &dst))) return s;
+    int used = 0;
+    SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
+        return launch_dot3<decltype(nv)::value>(c->dm, r, r2, part, 152 * 64 / 3, &used, c->stream);
+    }));
+    k_learn_theta<<<1, 256, 0, c->stream>>>(part, used, c->learned_step == 1 ? 1 : 0, dst);
+    SEM_CUDA(cudaGetLastError());
+    k_learn_step<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, zx, zl, dst, z);
+    SEM_CUDA(cudaGetLastError());
+    c->stats.kernel_launches += 2;
+    SEM_CUDA(cudaMemcpyAsync(c->h_lstat, dst, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->stream));
     c->stats.learned_guesses++;
-    double ratio = 1.0;
-    if (theta > 0 && n_ext > 0) {
-        k_axpby<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, 1.0 - theta, zx, theta, zl, z);
-        c->stats.kernel_launches++;
-        SEM_CUDA(cudaGetLastError());
-        c->stats.learned_accepted++;
-        const double n_t = n_ext - 2.0 * theta * (n_ext - rx) + theta * theta * den;  // |r_ext - theta A d|^2
-        ratio = std::sqrt(std::max(0.0, n_t) / n_ext);
-    }
-    c->stats.last_guess_residual_ratio = ratio;
-    c->stats.last_guess_theta = theta;
-    c->stats.learned_ratio_sum += ratio;
+    c->lr_pending = true;
+    return SEM_OK;
+}
+
+// statistics of the last learned step, once the stream has passed it (the
+// stage solve's read-back synchronises the stream)
+static int learned_collect(sem_ctx* c)
+{
+    if (!c->lr_pending) return SEM_OK;
+    SEM_CUDA(cudaStreamSynchronize(c->stream));  // a no-op after the solve's read-back
+    const double* h = c->h_lstat;
+    c->lr_nrm2 = h[0];
+    c->stats.last_guess_theta = h[1];
+    c->stats.last_guess_residual_ratio = h[2];
+    c->stats.learned_ratio_sum += h[2];
+    if (h[3] != 0.0) c->stats.learned_accepted++;
+    c->lr_pending = false;
     return SEM_OK;
 }
 
@@ -1968,6 +2049,7 @@ extern "C" int sem_ctx_set_learner(sem_ctx* c, sem_learner* L)
             return fail(SEM_ERR_ARG, "learner shape must be 4 N^2 -> 2 N^2 for this mesh");
     }
     c->learner = L;
+    c->lr_nrm2 = -1.0;
     return SEM_OK;
 }
 
@@ -2184,6 +2266,7 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
         sig[1] != c->hist_sig[1]) {
         c->hist_steps = 0;
         c->proj_count = c->proj_head = 0;
+        c->lr_nrm2 = -1.0;
     }
     const bool proj = extrap && c->proj_k > 0;
     double* pslots = nullptr;
@@ -2281,7 +2364,9 @@ static int schro_sdirk(sem_ctx* c, int stages, double* psi_re, double* psi_im, c
             }
             sem_solver_results res{};
             int sw = 1;
-            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw))) return s;
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw)) ||
+                (s = learned_collect(c)))
+                return s;
             c->stats.last_stage_iters[st] = res.n_iter;
             c->stats.last_stage_sweeps[st] = sw;
             if (rec && res.success) {
@@ -2412,7 +2497,9 @@ extern "C" int sem_schrodinger_dirk4s5_adaptive(sem_ctx* c, double* psi_re, doub
             }
             sem_solver_results res{};
             int sw = 1;
-            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw))) return s;
+            if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw)) ||
+                (s = learned_collect(c)))
+                return s;
             c->stats.last_stage_iters[st] = res.n_iter;
             c->stats.last_stage_sweeps[st] = sw;
             if (!res.success) ok = false;

@@ -310,12 +310,13 @@ __global__ void k_features(DevMesh m, const double* __restrict__ r, const double
     }
     const double rho = fmax(sqrt(s / (2.0 * NN)), rho_floor);
     const double inv = 1.0 / rho;
+    const double inv_alpha = 1.0 / alpha;  // one FP64 division per thread, not per node
     __nv_bfloat16* row = x + (long long)e * 4 * NN;
     for (int k = lane; k < NN; k += 32) {
         row[k] = __float2bfloat16((float)(r[base + k] * inv));
         row[NN + k] = __float2bfloat16((float)(r[n + base + k] * inv));
         row[2 * NN + k] = __float2bfloat16((float)(alpha * V[base + k]));
-        row[3 * NN + k] = __float2bfloat16((float)(m.mass[base + k] / alpha));
+        row[3 * NN + k] = __float2bfloat16((float)(m.mass[base + k] * inv_alpha));
     }
     if (lane == 0) sigma[e] = (float)(rho * NN / ms);
 }

@@ -266,8 +266,9 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
     __shared__ uint64_t bar[2];
     __shared__ uint32_t tmem_base;
     constexpr int ABYTES = TC_M * TC_BK * 2, BBYTES = BN * TC_BK * 2;
-    unsigned char* sA[2] = {tsm, tsm + ABYTES + BBYTES};
-    unsigned char* sB[2] = {tsm + ABYTES, tsm + 2 * ABYTES + BBYTES};
+    // stage b: A tile at tsm + b (ABYTES + BBYTES), its B tile right after
+    auto sA = [&](int b) { return tsm + (size_t)b * (ABYTES + BBYTES); };
+    auto sB = [&](int b) { return tsm + (size_t)b * (ABYTES + BBYTES) + ABYTES; };
     const int m0 = blockIdx.y * TC_M, n0 = blockIdx.x * BN;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (warp == 0) {
@@ -295,12 +296,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
             ok = false;
             break;
         }
-        tc_stage<BN>(g, sA[b], sB[b], m0, n0, kt * TC_BK);
+        tc_stage<BN>(g, sA(b), sB(b), m0, n0, kt * TC_BK);
         fence_proxy_async_smem();  // the staged tile is read by the tensor cores (async proxy)
         __syncthreads();
         if (threadIdx.x == 0) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            const uint32_t a0 = smem_addr(sA[b]), b0 = smem_addr(sB[b]);
+            const uint32_t a0 = smem_addr(sA(b)), b0 = smem_addr(sB(b));
 #pragma unroll
             for (int ks = 0; ks < TC_BK / 16; ++ks) {
                 const uint64_t ad = tc_desc(a0 + ks * TC_M * 32, 128, 256);
@@ -335,13 +336,24 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
                 : "memory");
             asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
             if (m < g.M) {
+                // every load of the chunk (bias, accumulated C) before its
+                // first store: the stores may alias them as far as the
+                // compiler knows, which would serialise load after store
+                float cin[16], bin[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const int nn = n0 + c0 + j;
+                    const bool in = nn < g.N;
+                    cin[j] = (in && g.accumulate) ? g.C[(long long)m * g.ldc + nn] : 0.f;
+                    bin[j] = (in && g.bias) ? __ldg(g.bias + nn) : 0.f;
+                }
 #pragma unroll
                 for (int j = 0; j < 16; ++j) {
                     const int nn = n0 + c0 + j;
                     if (nn >= g.N) continue;
                     float v = __uint_as_float(r[j]);
-                    if (g.accumulate) v += g.C[(long long)m * g.ldc + nn];
-                    if (g.bias) v += g.bias[nn];
+                    if (g.accumulate) v += cin[j];
+                    if (g.bias) v += bin[j];
                     if (g.relu) v = fmaxf(v, 0.f);
                     g.C[(long long)m * g.ldc + nn] = v;
                     if (g.Cbf) g.Cbf[(long long)m * g.ldc + nn] = __float2bfloat16(v);
