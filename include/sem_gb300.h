@@ -373,8 +373,12 @@ int sem_gemm_bf16(int M, int N, int K, const void* A, const void* B, float* C, v
 /* (no counterpart in the reference) Tensor-core instruction path of every
  * GEMM of the learned-guess network and of sem_gemm_bf16, process-wide:
  * 1 (default) tcgen05.mma with the accumulator in tensor memory (M = 128
- * per CTA, BF16 operands from shared memory, FP32 accumulation), 0 the
- * warp-level mma.sync m16n8k16 kernel.  Both compute in BF16 x BF16 -> FP32. */
+ * per CTA, BF16 operands from shared memory, FP32 accumulation), and the
+ * network's inference pass (sem_learner_forward) fused into one launch that
+ * chains the three layers through tensor and shared memory when the hidden
+ * and output widths are at most 256; 2 the same tcgen05 GEMMs one layer per
+ * launch; 0 the warp-level mma.sync m16n8k16 kernel.  All compute in
+ * BF16 x BF16 -> FP32 with BF16 hidden activations. */
 int sem_gemm_set_path(int path);
 /* (no counterpart in the reference) *expired = 1 when a bounded wait of a
  * tcgen05 GEMM ever ran out in this process (its output tile was then left

@@ -369,7 +369,206 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(BN) : "memory");
 }
 
-// GEMM path: 1 (default) the tcgen05 kernel, 0 the warp-level mma.sync kernel
+// ------------------------------------------------ fused forward pass
+// The network's inference pass in one kernel: per CTA 128 rows, the three
+// layers chained through tensor memory and shared memory.  Layer 1 streams
+// its A tile (the BF16 features) and every layer streams its weights
+// (transposed BF16 copies, K contiguous) in 64-wide K chunks through two
+// shared-memory buffers; the hidden activations never leave the SM: the
+// epilogue of layers 1 and 2 reads the FP32 accumulator with tcgen05.ld,
+// adds the bias, applies ReLU, rounds to BF16 and writes them in the
+// canonical K-major layout as the next layer's A operand (H, all 256 K at
+// once).  Accumulators: layer 1 in TMEM columns [0, H), layer 2 in
+// [256, 256 + H), layer 3 in [0, d_out rounded up to 16).  Same BF16
+// rounding points and MMA shapes as the per-layer GEMMs (M = 128, K = 16
+// steps in order), so the results agree with them.  Shapes: H <= 256 and
+// H, d_out <= 256; otherwise the per-layer GEMMs run.
+constexpr int MF_BUF = 48 * 1024;  // one staging buffer: A chunk (16 KB) + B chunk (<= 32 KB)
+constexpr int MF_H = 64 * 1024;    // hidden activations, 128 rows x 256 K BF16
+constexpr size_t MF_SMEM = 2 * (size_t)MF_BUF + MF_H;
+
+struct MlpArgs {
+    int rows, d_in, H, d_out;
+    const __nv_bfloat16* x;       // rows x d_in
+    const __nv_bfloat16* WT[3];   // [out][in]
+    const float* b[3];
+    float* out;                   // rows x d_out
+};
+
+__device__ __forceinline__ int mf_round16(int n) { return (n + 15) & ~15; }
+
+// stage K chunk k0 of layer l: B rows [0, nrows_pad) of WT (rows >= n are
+// zero), and for layer 1 the A rows of the CTA's x tile
+__device__ __forceinline__ void mf_stage(const MlpArgs& a, int l, int m0, int k0, unsigned char* buf)
+{
+    const int K = l == 0 ? a.d_in : a.H;
+    const int n = l == 2 ? a.d_out : a.H;
+    const int npad = mf_round16(n);
+    const __nv_bfloat16* W = l == 0 ? a.WT[0] : l == 1 ? a.WT[1] : a.WT[2];  // no runtime index into the parameters
+    unsigned char* sA = buf;
+    unsigned char* sB = buf + TC_M * TC_BK * 2;
+    const int nqa = l == 0 ? TC_M * (TC_BK / 8) : 0;
+    const int nq = nqa + npad * (TC_BK / 8);
+    for (int q0 = threadIdx.x; q0 < nq; q0 += 4 * TC_THREADS) {
+        uint32_t w[4][4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * TC_THREADS;
+            w[u][0] = w[u][1] = w[u][2] = w[u][3] = 0u;
+            if (q >= nq) continue;
+            const bool isA = q < nqa;
+            const int qq = isA ? q : q - nqa;
+            const int r = qq >> 3, kc = qq & 7;
+            const int k = k0 + kc * 8;
+            const int row = isA ? m0 + r : r;
+            const bool in = isA ? row < a.rows : row < n;
+            const int kvalid = in ? min(8, K - k) : 0;
+            if (kvalid <= 0) continue;
+            if (isA)
+                tc_chunk(a.x, 1, (long long)row * a.d_in + k, 1, kvalid, w[u]);
+            else
+                tc_chunk(W, 1, (long long)row * K + k, 1, kvalid, w[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int q = q0 + u * TC_THREADS;
+            if (q >= nq) continue;
+            const bool isA = q < nqa;
+            const int qq = isA ? q : q - nqa;
+            const int r = qq >> 3, kc = qq & 7;
+            unsigned char* dst = isA ? sA + tc_off(TC_M, r, kc * 8) : sB + tc_off(npad, r, kc * 8);
+            *(uint4*)dst = make_uint4(w[u][0], w[u][1], w[u][2], w[u][3]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(TC_THREADS) k_mlp_fwd(MlpArgs a, long long timeout_ns)
+{
+    extern __shared__ __align__(1024) unsigned char msm[];
+    __shared__ uint64_t bar[2];
+    __shared__ uint32_t tmem_base;
+    unsigned char* hbuf = msm + 2 * MF_BUF;
+    const int m0 = blockIdx.x * TC_M;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(&tmem_base)),
+                     "r"(512)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        mbar_fence_init();
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t taddr = tmem_base;
+    bool ok = true;
+    int g = 0;  // K chunks issued so far (all layers): buffer g & 1
+    const int row = m0 + warp * 32 + lane;
+    for (int l = 0; l < 3 && ok; ++l) {
+        const int K = l == 0 ? a.d_in : a.H;
+        const int n = l == 2 ? a.d_out : a.H;
+        const int npad = mf_round16(n);
+        const uint32_t idesc = tc_idesc(TC_M, npad);
+        const uint32_t acc_col = l == 1 ? 256u : 0u;
+        const int nk = (K + TC_BK - 1) / TC_BK;
+        for (int kt = 0; kt < nk && ok; ++kt, ++g) {
+            const int b = g & 1;
+            unsigned char* buf = msm + (size_t)b * MF_BUF;
+            if (g >= 2) ok = mbar_wait(&bar[b], (uint32_t)(((g - 2) >> 1) & 1), timeout_ns);
+            if (!__syncthreads_and(ok)) {
+                ok = false;
+                break;
+            }
+            mf_stage(a, l, m0, kt * TC_BK, buf);
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                const uint32_t b0 = smem_addr(buf + TC_M * TC_BK * 2);
+                // layer 1: A from the staged chunk; layers 2 and 3: from H
+                const uint32_t a0 = l == 0 ? smem_addr(buf) : smem_addr(hbuf) + (uint32_t)(kt * 4) * (TC_M * 32);
+#pragma unroll
+                for (int ks = 0; ks < TC_BK / 16; ++ks) {
+                    if (kt * TC_BK + ks * 16 >= mf_round16(K)) break;
+                    const uint64_t ad = tc_desc(a0 + ks * TC_M * 32, 128, 256);
+                    const uint64_t bd = tc_desc(b0 + ks * npad * 32, 128, 256);
+                    const uint32_t accf = (kt > 0 || ks > 0) ? 1u : 0u;
+                    asm volatile(
+                        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+                        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(taddr + acc_col),
+                        "l"(ad), "l"(bd), "r"(idesc), "r"(accf)
+                        : "memory");
+                }
+                asm volatile(
+                    "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                        smem_addr(&bar[b]))
+                    : "memory");
+            }
+        }
+        if (!ok) break;
+        // the layer's last commit covers every MMA issued before it
+        ok = mbar_wait(&bar[(g - 1) & 1], (uint32_t)(((g - 1) >> 1) & 1), timeout_ns);
+        ok = __syncthreads_and(ok) != 0;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (!ok) break;
+        // epilogue: 16 accumulator columns at a time
+        for (int c0 = 0; c0 < n; c0 += 16) {
+            uint32_t r[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                "[%16];"
+                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+                  "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+                  "=r"(r[15])
+                : "r"(taddr + acc_col + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0)
+                : "memory");
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+            const float* bias = l == 0 ? a.b[0] : l == 1 ? a.b[1] : a.b[2];
+            float bv[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) bv[j] = (c0 + j < n) ? __ldg(bias + c0 + j) : 0.f;
+            if (l < 2) {
+                // ReLU, BF16, into H at (row - m0, k = c0 + j); columns >= n
+                // (up to the 16-aligned K of the next layer) hold zeros
+                uint32_t pk[8];
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    const float v0 = (c0 + 2 * j < n) ? fmaxf(__uint_as_float(r[2 * j]) + bv[2 * j], 0.f) : 0.f;
+                    const float v1 =
+                        (c0 + 2 * j + 1 < n) ? fmaxf(__uint_as_float(r[2 * j + 1]) + bv[2 * j + 1], 0.f) : 0.f;
+                    pk[j] = pack_bf16(__float2bfloat16(v0), __float2bfloat16(v1));
+                }
+                const int rl = warp * 32 + lane;
+                *(uint4*)(hbuf + tc_off(TC_M, rl, c0)) = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+                *(uint4*)(hbuf + tc_off(TC_M, rl, c0 + 8)) = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            } else if (row < a.rows) {
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (c0 + j < n) a.out[(long long)row * n + c0 + j] = __uint_as_float(r[j]) + bv[j];
+            }
+        }
+        if (l < 2) {
+            // H complete before the next layer's MMAs read it (async proxy);
+            // this layer's accumulator reads are done
+            fence_proxy_async_smem();
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncthreads();
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        }
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(&g_tc_err, 1);
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(512) : "memory");
+}
+
+// GEMM path: 1 (default) the tcgen05 kernel and the fused inference pass,
+// 2 the tcgen05 kernel per layer, 0 the warp-level mma.sync kernel
 int g_gemm_path = 1;
 
 cudaError_t gemm(const GemmArgs& g, cudaStream_t st)
@@ -627,20 +826,58 @@ extern "C" int sem_learner_set_params(sem_learner* L, int l, const float* W, con
     return SEM_OK;
 }
 
-// x: rows x d_in (device, BF16) -> L->out (FP32, rows x d_out)
+// transposed BF16 weights [out][in] for the forward pass, rebuilt after an
+// update
+static int refresh_wt(sem_learner* L)
+{
+    if (!L->wt_dirty) return SEM_OK;
+    for (int l = 0; l < 3; ++l) {
+        const long long nw = (long long)L->din(l) * L->dout_(l);
+        k_transpose_bf16<<<g1d(nw), 256, 0, L->stream>>>(L->din(l), L->dout_(l), L->Wbf[l], L->WbfT[l]);
+    }
+    LCUDA(cudaGetLastError());
+    L->wt_dirty = false;
+    L->forward_launches += 3;
+    return SEM_OK;
+}
+
+// the fused inference pass applies (tcgen05 path, hidden and output widths
+// within one accumulator each)
+static bool fused_forward_ok(const sem_learner* L)
+{
+    return g_gemm_path == 1 && L->H <= 256 && L->d_out <= 256;
+}
+
+// inference: x (rows x d_in, BF16) -> out (rows x d_out, FP32) in one launch
+static int forward_fused(sem_learner* L, int rows, const __nv_bfloat16* x, float* out)
+{
+    int s = refresh_wt(L);
+    if (s) return s;
+    MlpArgs a{};
+    a.rows = rows;
+    a.d_in = L->d_in;
+    a.H = L->H;
+    a.d_out = L->d_out;
+    a.x = x;
+    a.out = out;
+    for (int l = 0; l < 3; ++l) {
+        a.WT[l] = L->WbfT[l];
+        a.b[l] = L->b[l];
+    }
+    LCUDA(cudaFuncSetAttribute(k_mlp_fwd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MF_SMEM));
+    k_mlp_fwd<<<(rows + TC_M - 1) / TC_M, TC_THREADS, MF_SMEM, L->stream>>>(a, 2000000000LL);
+    LCUDA(cudaGetLastError());
+    L->forward_launches += 1;
+    return SEM_OK;
+}
+
+// x: rows x d_in (device, BF16) -> L->out (FP32, rows x d_out), keeping
+// the hidden activations for the backward pass
 static int forward(sem_learner* L, int rows, const __nv_bfloat16* x)
 {
     int s = ensure_rows(L, rows);
     if (s) return s;
-    if (L->wt_dirty) {
-        for (int l = 0; l < 3; ++l) {
-            const long long nw = (long long)L->din(l) * L->dout_(l);
-            k_transpose_bf16<<<g1d(nw), 256, 0, L->stream>>>(L->din(l), L->dout_(l), L->Wbf[l], L->WbfT[l]);
-        }
-        LCUDA(cudaGetLastError());
-        L->wt_dirty = false;
-        L->forward_launches += 3;
-    }
+    if ((s = refresh_wt(L))) return s;
     // B(k, n) = W[k][n] = WT[n][k]: K contiguous
     GemmArgs g{};
     g.M = rows; g.N = L->H; g.K = L->d_in;
@@ -664,6 +901,8 @@ long long learner_forward_launches(const sem_learner* L) { return L ? L->forward
 extern "C" int sem_learner_forward(sem_learner* L, int rows, const void* x_bf16, float* out)
 {
     if (!L || rows < 0 || !x_bf16 || !out) return ctx_fail(SEM_ERR_ARG, "bad forward arguments");
+    if (rows == 0) return SEM_OK;
+    if (fused_forward_ok(L)) return forward_fused(L, rows, (const __nv_bfloat16*)x_bf16, out);
     int s = forward(L, rows, (const __nv_bfloat16*)x_bf16);
     if (s) return s;
     LCUDA(cudaMemcpyAsync(out, L->out, (size_t)rows * L->d_out * 4, cudaMemcpyDeviceToDevice, L->stream));
@@ -823,7 +1062,8 @@ extern "C" int sem_learner_fit(sem_learner* L, const void* X, const float* T, lo
 
 extern "C" int sem_gemm_set_path(int path)
 {
-    if (path != 0 && path != 1) return ctx_fail(SEM_ERR_ARG, "gemm path must be 0 (mma.sync) or 1 (tcgen05)");
+    if (path < 0 || path > 2)
+        return ctx_fail(SEM_ERR_ARG, "gemm path must be 0 (mma.sync), 1 (tcgen05, fused inference) or 2 (tcgen05)");
     g_gemm_path = path;
     return SEM_OK;
 }

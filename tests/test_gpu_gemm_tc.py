@@ -73,3 +73,35 @@ def test_learner_gradients_same_on_both_paths(semlib):
     for l in range(3):
         for a, b in zip(out[0][1][l], out[1][1][l]):
             assert np.abs(a - b).max() <= 1e-4 * max(np.abs(a).max(), 1e-12)
+
+
+@pytest.mark.parametrize("rows,d_in,hidden,d_out", [(4096, 324, 256, 162), (1000, 100, 96, 50), (129, 676, 256, 256),
+                                                    (1, 36, 16, 18), (300, 324, 200, 162)])
+def test_fused_forward_matches_per_layer_gemms(semlib, rows, d_in, hidden, d_out):
+    """the one-launch inference pass (three layers chained through tensor
+    memory and shared memory) against the per-layer tcgen05 GEMMs with their
+    BF16 activations in global memory, and against the mma.sync kernel"""
+    import torch
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.learned import Learner
+    L = capi.load()
+    g = torch.Generator(device="cuda").manual_seed(rows + d_in + hidden + d_out)
+    X = torch.randn(rows, d_in, generator=g, device="cuda").to(torch.bfloat16)
+    net = Learner(d_in, hidden, d_out, seed=9)
+    out = {}
+    try:
+        for path in (1, 2, 0):
+            capi.check(L.sem_gemm_set_path(path), "sem_gemm_set_path")
+            out[path] = net.forward(X).double()
+            torch.cuda.synchronize()
+    finally:
+        capi.check(L.sem_gemm_set_path(1), "sem_gemm_set_path")
+    scale = out[2].abs().max().clamp_min(1e-30)
+    assert bool(torch.isfinite(out[1]).all())
+    assert float((out[1] - out[2]).abs().max() / scale) < 1e-5
+    # mma.sync rounds the same products in another order; a BF16 hidden value
+    # may then round to its neighbour
+    assert float((out[1] - out[0]).abs().max() / scale) < 2e-2
+    e = C.c_int(-1)
+    capi.check(L.sem_gemm_check_error(C.byref(e)), "sem_gemm_check_error")
+    assert e.value == 0
