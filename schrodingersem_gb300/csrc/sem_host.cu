@@ -144,12 +144,12 @@ __global__ void k_lincomb_n(long long n, PtrList L, double* __restrict__ out)
     }
 }
 
-// Step length of the learned guess from launch_dot3's partials of
-// (r_ext.r_ext, r_ext.r_l, r_l.r_l), summed in a fixed order: the step theta
-// along d = z_l - z_ext minimising |r_ext - theta A d| (A d = r_ext - r_l),
-// or the whole step when full_step and the prediction is finite and raises
-// the residual at most tenfold.  st = (|r_ext|^2, theta, residual ratio,
-// accepted 1/0).
+// Step length of the learned guess from launch_dot3_f32's partials of
+// (r_ext.r_ext, r_ext.Ad, Ad.Ad), summed in a fixed order: the step theta
+// along d = z_l - z_ext minimising |r_ext - theta A d|, or the whole step
+// when full_step and the prediction is finite and raises the residual at
+// most tenfold (|r_l|^2 = |r_ext|^2 - 2 r_ext.Ad + |Ad|^2).
+// st = (|r_ext|^2, theta, residual ratio, accepted 1/0).
 __global__ void __launch_bounds__(256) k_learn_theta(const double* __restrict__ part, int used, int full_step,
                                                      double* __restrict__ st)
 {
@@ -171,14 +171,14 @@ __global__ void __launch_bounds__(256) k_learn_theta(const double* __restrict__ 
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        const double n_ext = red[0][0], rx = red[1][0], n_l = red[2][0];
-        const double den = n_ext - 2.0 * rx + n_l;
-        double theta = den > 0 ? (n_ext - rx) / den : 0.0;
+        const double n_ext = red[0][0], rad = red[1][0], den = red[2][0];
+        double theta = den > 0 ? rad / den : 0.0;
+        const double n_l = n_ext - 2.0 * rad + den;
         if (full_step && isfinite(n_l) && n_l <= 100.0 * n_ext) theta = 1.0;
         double ratio = 1.0, acc = 0.0;
         if (theta > 0 && n_ext > 0) {
             acc = 1.0;
-            const double n_t = n_ext - 2.0 * theta * (n_ext - rx) + theta * theta * den;  // |r_ext - theta A d|^2
+            const double n_t = n_ext - 2.0 * theta * rad + theta * theta * den;  // |r_ext - theta A d|^2
             ratio = sqrt(fmax(0.0, n_t) / n_ext);
         }
         st[0] = n_ext;
@@ -186,6 +186,14 @@ __global__ void __launch_bounds__(256) k_learn_theta(const double* __restrict__ 
         st[2] = ratio;
         st[3] = acc;
     }
+}
+
+// d = z_l - z_ext in FP32 (both planes)
+__global__ void k_diff_f32(long long n, const double* __restrict__ zl, const double* __restrict__ zx,
+                           float* __restrict__ d)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        d[i] = (float)(zl[i] - zx[i]);
 }
 
 // z = (1 - theta) z_ext + theta z_l when the step was accepted (st[3]);
@@ -1952,9 +1960,8 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     if ((s = launch_learn_op(c, a))) return s;
     if (!use) return SEM_OK;
     float* delta = nullptr;
-    double *zl = nullptr, *r2 = nullptr;
-    if ((s = wsget(c, "lr_delta", (size_t)c->E * 2 * NN, &delta)) || (s = wsget(c, "lr_zl", 2 * c->n, &zl)) ||
-        (s = wsget(c, "lr_r2", 2 * c->n, &r2)))
+    double* zl = nullptr;
+    if ((s = wsget(c, "lr_delta", (size_t)c->E * 2 * NN, &delta)) || (s = wsget(c, "lr_zl", 2 * c->n, &zl)))
         return s;
     const long long fl0 = learner_forward_launches(c->learner);
     if ((s = sem_learner_set_stream(c->learner, c->stream)) || (s = sem_learner_forward(c->learner, c->E, x, delta)))
@@ -1967,18 +1974,28 @@ static int learned_guess(sem_ctx* c, const double* V, double alpha, const double
     k.delta = delta;
     k.zo = zl;
     if ((s = launch_learn_op(c, k))) return s;
-    if ((s = guess_residual(c, V, alpha, b, zl, r2))) return s;
     // minimal residual along the predicted correction d = z_l - z_ext:
-    // r(theta) = r_ext - theta A d with A d = r_ext - r_l, so
-    // theta = r_ext.(r_ext - r_l) / |r_ext - r_l|^2 and |r(theta)| <= |r_ext|.
-    // The step is taken on the device (no read-back before the solve); its
-    // statistics are collected after the stage solve (learned_collect)
+    // r(theta) = r_ext - theta A d, so theta = r_ext.Ad / |Ad|^2 and
+    // |r(theta)| <= |r_ext|.  A d only sets the step length, so it is
+    // applied in FP32; the stage solve judges the guess on its true FP64
+    // residual.  The step is taken on the device (no read-back before the
+    // solve); its statistics are collected after it (learned_collect)
+    float *d32 = nullptr, *ad32 = nullptr, *v32 = nullptr;
+    if ((s = wsget(c, "lr_d32", 2 * c->n, &d32)) || (s = wsget(c, "lr_ad32", 2 * c->n, &ad32)) ||
+        (s = wsget(c, "lr_v32", c->n, &v32)))
+        return s;
+    k_diff_f32<<<grid_1d(2 * c->n), 256, 0, c->stream>>>(2 * c->n, zl, zx, d32);
+    SEM_CUDA(cudaGetLastError());
+    k_to_f32<<<grid_1d(c->n), 256, 0, c->stream>>>(c->n, V, v32);
+    SEM_CUDA(cudaGetLastError());
+    c->stats.kernel_launches += 2;
+    if ((s = sem_apply_schro_res_f32(c, v32, (float)alpha, d32, d32 + c->n, ad32, ad32 + c->n))) return s;
     double* part = nullptr;
     double* dst = nullptr;
     if ((s = wsget(c, "dot_part", 152 * 64, &part)) || (s = wsget(c, "lr_stat", 4, &dst))) return s;
     int used = 0;
     SEM_LAUNCH(dispatch_n(c->N, [&](auto nv) {
-        return launch_dot3<decltype(nv)::value>(c->dm, r, r2, part, 152 * 64 / 3, &used, c->stream);
+        return launch_dot3_f32<decltype(nv)::value>(c->dm, r, ad32, part, 152 * 64 / 3, &used, c->stream);
     }));
     k_learn_theta<<<1, 256, 0, c->stream>>>(part, used, c->learned_step == 1 ? 1 : 0, dst);
     SEM_CUDA(cudaGetLastError());

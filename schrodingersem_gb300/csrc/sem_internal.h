@@ -207,6 +207,10 @@ cudaError_t launch_dot(const DevMesh& m, const double* a, const double* b, doubl
 template <int N>
 cudaError_t launch_dot3(const DevMesh& m, const double* a, const double* b, double* part, int max_blocks,
                         int* blocks_used, cudaStream_t st);
+// the same with an FP32 second vector (FP64 sums)
+template <int N>
+cudaError_t launch_dot3_f32(const DevMesh& m, const double* a, const float* b, double* part, int max_blocks,
+                            int* blocks_used, cudaStream_t st);
 // out[n] = gather(p + sum_l c[l] z_l) for every node (unmask semantics); then
 // optional f-apply: y = L-closure of the combination.
 struct ZList {

@@ -473,9 +473,9 @@ cudaError_t launch_mask(const DevMesh& m, bool fp32, void* a, cudaStream_t st)
 }
 
 // three owner-weighted dots of two-plane vectors at once: part[3 blk + q] =
-// (a.a, a.b, b.b) over both planes (fixed order)
-template <int N>
-__global__ void k_dot3(DevMesh m, const double* __restrict__ a, const double* __restrict__ b, double* part)
+// (a.a, a.b, b.b) over both planes (fixed order), FP64 sums; b FP64 or FP32
+template <int N, typename TB>
+__global__ void k_dot3(DevMesh m, const double* __restrict__ a, const TB* __restrict__ b, double* part)
 {
     __shared__ double red[34];
     constexpr int NN = N * N;
@@ -488,7 +488,7 @@ __global__ void k_dot3(DevMesh m, const double* __restrict__ a, const double* __
         if (ni_owner(ni)) {
 #pragma unroll
             for (int q = 0; q < 2; ++q) {
-                const double x = a[q * m.n + idx], y = b[q * m.n + idx];
+                const double x = a[q * m.n + idx], y = (double)b[q * m.n + idx];
                 s0 = fma(x, x, s0);
                 s1 = fma(x, y, s1);
                 s2 = fma(y, y, s2);
@@ -511,7 +511,17 @@ cudaError_t launch_dot3(const DevMesh& m, const double* a, const double* b, doub
 {
     const int grid = grid_for(m.n, 256, max_blocks);
     *blocks_used = grid;
-    k_dot3<N><<<grid, 256, 0, st>>>(m, a, b, part);
+    k_dot3<N, double><<<grid, 256, 0, st>>>(m, a, b, part);
+    return cudaGetLastError();
+}
+
+template <int N>
+cudaError_t launch_dot3_f32(const DevMesh& m, const double* a, const float* b, double* part, int max_blocks,
+                            int* blocks_used, cudaStream_t st)
+{
+    const int grid = grid_for(m.n, 256, max_blocks);
+    *blocks_used = grid;
+    k_dot3<N, float><<<grid, 256, 0, st>>>(m, a, b, part);
     return cudaGetLastError();
 }
 
@@ -601,6 +611,8 @@ cudaError_t launch_learn(const DevMesh& m, const LearnArgs& a, cudaStream_t st)
                                         int*, cudaStream_t);                                         \
     template cudaError_t launch_dot3<NV>(const DevMesh&, const double*, const double*, double*, int, \
                                          int*, cudaStream_t);                                        \
+    template cudaError_t launch_dot3_f32<NV>(const DevMesh&, const double*, const float*, double*,   \
+                                             int, int*, cudaStream_t);                               \
     template cudaError_t launch_combo_f<NV>(const DevMesh&, const double*, const double*,            \
                                             const ZList&, double*, cudaStream_t);                    \
     template cudaError_t launch_update<NV>(const DevMesh&, const double*, const ZList&, double*,     \
