@@ -83,8 +83,10 @@ enum sem_option {
                                     to what the outer test still needs (x 0.3), 0 always
                                     SEM_OPT_INNER_TOL */
     SEM_OPT_LEARNED_STEP = 15,   /* SEM_GUESS_LEARNED: 0 (default) move from the base guess along
-                                    the predicted correction by the step that minimises the FP64
-                                    residual; 1 take the whole predicted correction (the MINRES
+                                    the predicted correction by the step that minimises the
+                                    residual (FP32 apply of the correction against the base
+                                    guess's FP64 residual); 1 take the whole predicted
+                                    correction (the MINRES
                                     solve removes its high-frequency error quickly), unless its
                                     residual is not finite or more than 10x the base's */
     SEM_OPT_PROJECT = 14,        /* mixed mode with SEM_GUESS_EXTRAPOLATE / _LEARNED, SDIRK
