@@ -86,9 +86,9 @@ enum sem_option {
                                     the predicted correction by the step that minimises the
                                     residual (FP32 apply of the correction against the base
                                     guess's FP64 residual); 1 take the whole predicted
-                                    correction (the MINRES
-                                    solve removes its high-frequency error quickly), unless its
-                                    residual is not finite or more than 10x the base's */
+                                    correction (the MINRES solve removes its high-frequency
+                                    error quickly), unless its residual is not finite or more
+                                    than 10x the base's */
     SEM_OPT_PROJECT = 14,        /* mixed mode with SEM_GUESS_EXTRAPOLATE / _LEARNED, SDIRK
                                     drivers: K in 1..24 replaces the extrapolation by the
                                     projection onto the last K stage solutions (the guess
