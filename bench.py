@@ -28,8 +28,10 @@ Further legs (each also a JSON key of the headline line unless skipped):
   batch   the ensemble of 1,024 seeded BDF2 instances (one persistent launch
           per step, a replayed CUDA graph)
   --leg c4   learned stage guess on SDIRK4-5, 128x128, p = 8 (own JSON line)
-  --leg c5   adaptive SDIRK4-5 on 384x384, p = 12 (21.2 M nodes) with a CPU
-             oracle replay of its first accepted step (own JSON line)
+  --leg c5   adaptive SDIRK4-5 on 384x384, p = 12 (21.2 M nodes), extrapolated
+             and learned stage guesses (the network trained on the run's own
+             recorded stages), with an FP64 replay of its first accepted
+             step (own JSON line)
   --profile-case   small cases for ncu captures of single kernels
 """
 from __future__ import annotations
@@ -1215,18 +1217,27 @@ def c5_fields(X, Y):
 def run_c5(a):
     """Adaptive SDIRK4-5 (embedded error 1e-8) on 384x384 jittered quads over
     [-12,12]^2 at p = 12 (4609^2 = 21.2 M global nodes), FP32 inner + FP64
-    refinement, element preconditioner, extrapolated stage guess, for
-    --c5-steps accepted steps.  The CPU oracle then replays the first
-    accepted step with the same dt (fixed-step SDIRK4-5, MINRES 1e-12) from
-    the same initial state, and the GPU's state after that step is compared
-    with it."""
+    refinement, element preconditioner, for --c5-steps accepted steps in
+    each form of --c5-forms: the scaled stage of the last accepted step as
+    the stage guess ("extrapolated"), and that guess corrected by the
+    network ("learned").  The network is trained first on rows recorded
+    from the adaptive run's own stages (--c5-train-steps accepted steps
+    after skipping --c5-train-skip, so that dt has left the trial step).
+    The plain FP64 solver (and with --c5-cpu-replay the CPU oracle) then
+    replays the first accepted step with the same dt from the same initial
+    state, and the GPU's state after that step is compared with it."""
     import torch
 
     import schrodingersem_gb300 as S
     from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.learned import Learner
     from schrodingersem_gb300.meshgen import structured_quads
     S.build()
     n, p = a.c5_n, a.c5_p
+    forms = [f for f in a.c5_forms.split(",") if f]
+    for f in forms:
+        if f not in ("extrapolated", "learned"):
+            raise SystemExit(f"unknown c5 form {f}")
     t0 = time.time()
     co, el = structured_quads(n, box=(-12.0, 12.0, -12.0, 12.0), jitter=0.1, seed=1)
     ctx = S.Context(p, coords=co, elements=el)
@@ -1244,42 +1255,88 @@ def run_c5(a):
     ctx.set_option(capi.OPT_REFINE_TOL_SCALE, 0.1)
     ctx.set_option(capi.OPT_PROFILE, 1)
     dV = ctx.to_device(V)
-    # the first accepted step alone, kept for the CPU replay
+    maxit = 20 * ctx.dof()
+    # the first accepted step alone, kept for the replays
     d1r, d1i = ctx.to_device(re), ctx.to_device(im)
-    ok1, dts1, _ = ctx.schrodinger_adaptive(d1r, d1i, dV, 1e9, a.c5_dt0 / 2, 20 * ctx.dof(), 1e-10, a.c5_err,
-                                            n_steps=1)
+    ok1, dts1, _ = ctx.schrodinger_adaptive(d1r, d1i, dV, 1e9, a.c5_dt0 / 2, maxit, 1e-10, a.c5_err, n_steps=1)
     first = (d1r.cpu().numpy(), d1i.cpu().numpy(), float(dts1[0]))
     del d1r, d1i
-    dre, dim = ctx.to_device(re), ctx.to_device(im)
-    s0 = ctx.stats()
+    training = None
+    if "learned" in forms:
+        # skip the controller's first steps, then record the stages of a few
+        # accepted steps (the first step of that call has no previous stage
+        # and gives no rows)
+        t2 = time.time()
+        tr, ti = ctx.to_device(re), ctx.to_device(im)
+        okt, dtt, _ = ctx.schrodinger_adaptive(tr, ti, dV, 1e9, a.c5_dt0 / 2, maxit, 1e-10, a.c5_err,
+                                               n_steps=a.c5_train_skip, capacity=a.c5_train_skip + 10)
+        assert okt
+        ctx.record(a.c5_rows)
+        okt, dtr, _ = ctx.schrodinger_adaptive(tr, ti, dV, 1e9, float(dtt[-1]), maxit, 1e-10, a.c5_err,
+                                               n_steps=a.c5_train_steps, capacity=a.c5_train_steps + 10)
+        assert okt
+        Xd, Td = ctx.dataset()
+        ctx.record(0)
+        del tr, ti
+        record_s = time.time() - t2
+        t2 = time.time()
+        net = Learner.for_mesh(ctx.N, hidden=a.c5_hidden, seed=3)
+        loss = net.fit(Xd, Td, epochs=a.c5_epochs, batch=1024, lr=1e-3, seed=11)
+        torch.cuda.synchronize()
+        fit_s = time.time() - t2
+        tvar = float(Td.float().pow(2).mean())
+        training = {"rows": int(Xd.shape[0]), "skip_steps": a.c5_train_skip, "recorded_steps": a.c5_train_steps,
+                    "dt_workload_units": {"first": float(2 * dtr[0]), "last": float(2 * dtr[-1])},
+                    "record_s": record_s, "fit_s": fit_s, "epochs": a.c5_epochs, "hidden": a.c5_hidden,
+                    "params": net.d_in * net.hidden + net.hidden + net.hidden * net.hidden + net.hidden +
+                    net.hidden * net.d_out + net.d_out,
+                    "final_mse_rel": loss / tvar if tvar else None}
+        del Xd, Td
+        torch.cuda.empty_cache()
+        ctx.set_learner(net)
     st = torch.cuda.current_stream()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    t1 = time.time()
-    e0.record(st)
-    ok, dts, nrej = ctx.schrodinger_adaptive(dre, dim, dV, 1e9, a.c5_dt0 / 2, 20 * ctx.dof(), 1e-10, a.c5_err,
-                                             n_steps=a.c5_steps, capacity=a.c5_steps + 10)
-    e1.record(st)
-    torch.cuda.synchronize()
-    wall = time.time() - t1
-    ms = e0.elapsed_time(e1)
-    s1 = ctx.stats()
-    fin = (dre.cpu().numpy(), dim.cpu().numpy())
-    stages = 5 * (len(dts) + nrej)
+    res = {}
+    fin = None
+    for f in forms:
+        ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_LEARNED if f == "learned" else capi.GUESS_EXTRAPOLATE)
+        dre, dim = ctx.to_device(re), ctx.to_device(im)
+        s0 = ctx.stats()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t1 = time.time()
+        e0.record(st)
+        ok, dts, nrej = ctx.schrodinger_adaptive(dre, dim, dV, 1e9, a.c5_dt0 / 2, maxit, 1e-10, a.c5_err,
+                                                 n_steps=a.c5_steps, capacity=a.c5_steps + 10)
+        e1.record(st)
+        torch.cuda.synchronize()
+        wall = time.time() - t1
+        ms = e0.elapsed_time(e1)
+        s1 = ctx.stats()
+        fin = (dre.cpu().numpy(), dim.cpu().numpy())
+        del dre, dim
+        stages = 5 * (len(dts) + nrej)
+        r = {"s_per_step": ms / 1e3 / max(1, len(dts)), "accepted": int(len(dts)), "rejected": int(nrej),
+             "success": bool(ok), "wall_s": wall, "t_end_workload_units": float(2 * np.sum(dts)),
+             "dt_workload_units": {"first": float(2 * dts[0]), "last": float(2 * dts[-1]),
+                                   "min": float(2 * np.min(dts)), "max": float(2 * np.max(dts))},
+             "last_error_estimate": s1.last_error_estimate,
+             "inner_iterations_per_stage": (s1.solver_iterations_fp32 - s0.solver_iterations_fp32) / max(1, stages),
+             "solver_kernel_ms": s1.solver_kernel_ms - s0.solver_kernel_ms,
+             "norm_drift": abs(mass_norm(J, w, *fin) - 1.0)}
+        n_l = s1.learned_guesses - s0.learned_guesses
+        if n_l:
+            r["learned"] = {"guesses": int(n_l), "accepted": int(s1.learned_accepted - s0.learned_accepted),
+                            "mean_guess_residual_ratio": (s1.learned_ratio_sum - s0.learned_ratio_sum) / n_l}
+        res[f] = r
+    head = "learned" if "learned" in res else forms[0]
     out = {
-        "leg": "c5", "metric": "adaptive SDIRK4-5 seconds per accepted step", "value": ms / 1e3 / max(1, len(dts)),
-        "unit": "s/step", "accepted": int(len(dts)), "rejected": int(nrej), "success": bool(ok), "wall_s": wall,
-        "t_end_workload_units": float(2 * np.sum(dts)),
-        "dt_workload_units": {"first": float(2 * dts[0]), "last": float(2 * dts[-1]),
-                              "min": float(2 * np.min(dts)), "max": float(2 * np.max(dts))},
-        "last_error_estimate": s1.last_error_estimate,
-        "inner_iterations_per_stage": (s1.solver_iterations_fp32 - s0.solver_iterations_fp32) / max(1, stages),
-        "solver_kernel_ms": s1.solver_kernel_ms - s0.solver_kernel_ms, "setup_s": setup_s,
-        "norm_drift": abs(mass_norm(J, w, *fin) - 1.0),
+        "leg": "c5", "metric": "adaptive SDIRK4-5 seconds per accepted step", "value": res[head]["s_per_step"],
+        "unit": "s/step", "form": head, "forms": res, "training": training, "setup_s": setup_s,
         "config": {"workload": f"{n}x{n} jittered quads on [-12,12]^2, p={p} ({(n * p + 1) ** 2:,} nodes), double "
                                f"well + 0.5-amplitude Gaussian disorder, adaptive SDIRK4-5 at embedded error "
                                f"{a.c5_err:g}, MINRES 1e-10, FP32 inner + FP64 refinement, element preconditioner, "
-                               f"extrapolated stage guess", "local_nodes_per_component": ctx.n},
+                               f"stage guess: the last accepted step's stage scaled by the dt ratio, corrected by "
+                               f"the network in the learned form", "local_nodes_per_component": ctx.n},
     }
     # the first accepted step again with the plain FP64 solver (zero stage
     # guess, MINRES tolerance 1e-13, the reference's algorithm, pinned to the
@@ -1296,7 +1353,7 @@ def run_c5(a):
                           mass_norm(J, w, pr, pi),
                           "note": "the GPU's plain FP64 MINRES (the reference's algorithm, tolerance 1e-13) "
                                   "replays the first accepted step with the same dt"}
-    del dre, dim, dV, rr, ri
+    del dV, rr, ri
     ctx.close()
     torch.cuda.empty_cache()
     if a.c5_cpu_replay:
@@ -1403,6 +1460,12 @@ def main():
     ap.add_argument("--c5-steps", type=int, default=500)
     ap.add_argument("--c5-dt0", type=float, default=4e-4)
     ap.add_argument("--c5-err", type=float, default=1e-8)
+    ap.add_argument("--c5-forms", default="extrapolated,learned")
+    ap.add_argument("--c5-train-skip", type=int, default=20)
+    ap.add_argument("--c5-train-steps", type=int, default=4)
+    ap.add_argument("--c5-rows", type=int, default=2_000_000)
+    ap.add_argument("--c5-hidden", type=int, default=256)
+    ap.add_argument("--c5-epochs", type=int, default=4)
     ap.add_argument("--c5-cpu-replay", action="store_true",
                     help="also replay the first accepted step on the CPU oracle (hours at the full size)")
     ap.add_argument("--profile-case", choices=["minres", "apply", "batch"])

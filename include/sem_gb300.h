@@ -333,7 +333,10 @@ int sem_schrodinger_dirk4s3(sem_ctx* ctx, double* psi_re, double* psi_im, const 
  * dts (host, may be NULL) receives the accepted steps' dt, up to
  * dts_capacity of them (the sequence replays the fixed-step reference).  In
  * mixed precision with a stage guess other than SEM_GUESS_ZERO a stage starts
- * from the last accepted step's stage scaled by the dt ratio. */
+ * from the last accepted step's stage scaled by the dt ratio; with
+ * SEM_GUESS_LEARNED and a network set, the network corrects that guess as in
+ * the fixed-step drivers, and sem_ctx_record collects training rows from
+ * these stages too. */
 int sem_schrodinger_dirk4s5_adaptive(sem_ctx* ctx, double* psi_re, double* psi_im, const double* V,
                                      double T, const sem_solver_opts* opts, double err_tol,
                                      double* dts, int dts_capacity, int* n_accepted, int* n_rejected,
@@ -394,7 +397,8 @@ int sem_gemm_check_error(int* expired);
  * positive step lowers it). */
 int sem_ctx_set_learner(sem_ctx* ctx, sem_learner* learner);
 /* record training rows from the SDIRK drivers' stage solves (mixed precision,
- * SEM_GUESS_EXTRAPOLATE or _LEARNED, from the third step on) into a device
+ * SEM_GUESS_EXTRAPOLATE or _LEARNED, from the third step on; in the adaptive
+ * driver from the second accepted step on) into a device
  * dataset of capacity_rows rows; 0 stops recording.  Resets the dataset. */
 int sem_ctx_record(sem_ctx* ctx, long long capacity_rows);
 /* the recorded dataset: device pointers X (BF16 rows x d_in), T (FP32 rows x

@@ -2512,6 +2512,13 @@ extern "C" int sem_schrodinger_dirk4s5_adaptive(sem_ctx* c, double* psi_re, doub
             } else {
                 SEM_CUDA(cudaMemsetAsync(z, 0, sizeof(double) * 2 * c->n, c->stream));
             }
+            // learned correction of the scaled stage of the last step, and/or
+            // a training sample, as in the fixed-step drivers (the features
+            // carry alpha, so one network serves every dt of the run)
+            const bool rec = !x_zero && c->ds_cap > 0;
+            const bool use = !x_zero && c->guess == SEM_GUESS_LEARNED && c->learner;
+            double* zext = nullptr;
+            if ((rec || use) && (s = learned_guess(c, r.V, alpha, b, z, use, &zext, nullptr))) return s;
             sem_solver_results res{};
             int sw = 1;
             if ((s = schro_stage_solve(&r, alpha, b, z, o->max_iter, o->tol, x_zero, &res, &sw)) ||
@@ -2519,6 +2526,7 @@ extern "C" int sem_schrodinger_dirk4s5_adaptive(sem_ctx* c, double* psi_re, doub
                 return s;
             c->stats.last_stage_iters[st] = res.n_iter;
             c->stats.last_stage_sweeps[st] = sw;
+            if (rec && res.success && (s = record_sample(c, z, zext))) return s;
             if (!res.success) ok = false;
         }
         if (!ok) break;

@@ -179,6 +179,52 @@ def test_learned_stage_guess_in_driver(semlib, torch_mod):
     assert sum(lrn[2:]) <= 1.05 * sum(ext[2:])
 
 
+def test_learned_guess_in_adaptive_driver(semlib, torch_mod, oracle):
+    """adaptive SDIRK4-5 with the network: rows are recorded from the
+    adaptive run's stages, the fitted network corrects every stage guess
+    after the first accepted step, and the state still equals the oracle's
+    fixed-step replay of the accepted dt sequence to 1e-8"""
+    from schrodingersem_gb300 import capi
+    from schrodingersem_gb300.learned import Learner
+    ctx, packet, V = _case(semlib)
+    T, tol, err_tol, dt0 = 0.08, 1e-12, 1e-6, 0.02
+    ctx.set_option(capi.OPT_SOLVE_PRECISION, capi.PREC_MIXED)
+    ctx.set_option(capi.OPT_PRECOND, capi.PRECOND_FDM)
+    ctx.set_option(capi.OPT_REFINE_TOL_SCALE, 0.1)
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_EXTRAPOLATE)
+    ctx.record(ctx.E * 5 * 40)
+    for pk in (((-2.0, 1.0), 1.0, (2.0, 1.0)), ((1.0, -1.0), 0.7, (-3.0, 2.0))):
+        re, im = packet(*pk)
+        ok, dts, _ = ctx.schrodinger_adaptive(re, im, V, T, dt0, 100000, tol, err_tol)
+        assert ok and len(dts) >= 2
+    X, Tt = ctx.dataset()
+    ctx.record(0)
+    assert X.shape[0] > 0 and X.shape[0] % ctx.E == 0
+    assert X.shape[1] == 4 * ctx.N ** 2 and Tt.shape == (X.shape[0], 2 * ctx.N ** 2)
+    assert torch_mod.isfinite(Tt).all()
+    L = Learner.for_mesh(ctx.N, hidden=64, seed=3)
+    L.fit(X, Tt, epochs=10, batch=256, lr=1e-3, seed=5)
+    ctx.set_learner(L)
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_LEARNED)
+    re0, im0 = packet((-1.0, 0.5), 0.8, (3.0, -1.0))
+    a, b = re0.copy(), im0.copy()
+    s0 = ctx.stats()
+    ok, dts, nrej = ctx.schrodinger_adaptive(a, b, V, T, dt0, 100000, tol, err_tol)
+    s1 = ctx.stats()
+    assert ok and len(dts) >= 2
+    assert abs(dts.sum() - T) < 1e-12
+    n_l = s1.learned_guesses - s0.learned_guesses
+    assert 5 * (len(dts) - 1) <= n_l <= 5 * (len(dts) - 1 + nrej)
+    assert 0.0 <= s1.last_guess_residual_ratio <= 1.0
+    co, el = structured(8, box=(-4, 4, -4, 4), jitter=0.1, seed=2)  # the mesh of _case
+    om = oracle.Mesh(ctx.p, coords=co, elements=el)
+    r, i = re0.copy(), im0.copy()
+    for d in dts:
+        r, i, okk = om.schrodinger("dirk4s5", r, i, V, 0.5 * d, d, 100000, 1e-13)
+        assert okk
+    assert max(rel_err(a, r), rel_err(b, i)) < 1e-8
+
+
 def test_set_learner_checks_shape(semlib):
     from schrodingersem_gb300.capi import SemError
     from schrodingersem_gb300.learned import Learner
