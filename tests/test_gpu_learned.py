@@ -172,9 +172,11 @@ def test_learned_stage_guess_in_driver(semlib, torch_mod):
     mean_ratio = (s1.learned_ratio_sum - s0.learned_ratio_sum) / n_l
     print("extrapolated", ext, "learned", lrn, "accepted", s1.learned_accepted - s0.learned_accepted,
           "mean residual ratio", mean_ratio, "last theta", s1.last_guess_theta)
-    # what the network gains over the extrapolation alone: a stage guess with a
-    # clearly smaller FP64 residual at every stage where it runs (steps 3..),
-    # without costing iterations overall
+    # what the network gains over the extrapolation alone on this fixed-step
+    # case: a stage guess with a clearly smaller FP64 residual at every stage
+    # where it runs (steps 3..; measured 0.69 of the extrapolation's).  The
+    # iteration count does not follow here (measured 504 against 494 over
+    # steps 3..6), so the test only bounds the extra iterations at 5 %
     assert mean_ratio < 0.9
     assert sum(lrn[2:]) <= 1.05 * sum(ext[2:])
 
@@ -205,12 +207,28 @@ def test_learned_guess_in_adaptive_driver(semlib, torch_mod, oracle):
     L = Learner.for_mesh(ctx.N, hidden=64, seed=3)
     L.fit(X, Tt, epochs=10, batch=256, lr=1e-3, seed=5)
     ctx.set_learner(L)
-    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_LEARNED)
     re0, im0 = packet((-1.0, 0.5), 0.8, (3.0, -1.0))
+    # the same held-out packet with the scaled previous stage alone
+    e0 = ctx.stats()
+    ok, dts_e, nrej_e = ctx.schrodinger_adaptive(re0.copy(), im0.copy(), V, T, dt0, 100000, tol, err_tol)
+    e1 = ctx.stats()
+    assert ok
+    ctx.set_option(capi.OPT_STAGE_GUESS, capi.GUESS_LEARNED)
     a, b = re0.copy(), im0.copy()
     s0 = ctx.stats()
     ok, dts, nrej = ctx.schrodinger_adaptive(a, b, V, T, dt0, 100000, tol, err_tol)
     s1 = ctx.stats()
+    it_e = (e1.solver_iterations_fp32 - e0.solver_iterations_fp32) / (5 * (len(dts_e) + nrej_e))
+    it_l = (s1.solver_iterations_fp32 - s0.solver_iterations_fp32) / (5 * (len(dts) + nrej))
+    mean_ratio = (s1.learned_ratio_sum - s0.learned_ratio_sum) / max(1, s1.learned_guesses - s0.learned_guesses)
+    print("inner iterations per stage: scaled previous stage", it_e, "learned", it_l, "steps", len(dts_e),
+          len(dts), "mean residual ratio", mean_ratio)
+    # what the network gains here: a guess residual clearly below the scaled
+    # previous stage's (measured 0.65 of it) and fewer inner iterations per
+    # stage (measured 22.1 against 22.8; every kernel on this path reduces
+    # in a fixed order and the training is seeded, so the counts repeat)
+    assert mean_ratio < 0.8
+    assert it_l < it_e
     assert ok and len(dts) >= 2
     assert abs(dts.sum() - T) < 1e-12
     n_l = s1.learned_guesses - s0.learned_guesses
