@@ -289,6 +289,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
     constexpr uint32_t idesc = tc_idesc(TC_M, BN);
     const int nk = (g.K + TC_BK - 1) / TC_BK;
     bool ok = true;
+    int issued = 0;  // K chunks whose MMAs thread 0 has committed
     for (int kt = 0; kt < nk && ok; ++kt) {
         const int b = kt & 1;
         if (kt >= 2) ok = mbar_wait(&bar[b], (uint32_t)(((kt - 2) >> 1) & 1), timeout_ns);
@@ -317,6 +318,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
                              smem_addr(&bar[b]))
                          : "memory");
         }
+        issued = kt + 1;
     }
     if (ok && nk > 0) ok = mbar_wait(&bar[(nk - 1) & 1], (uint32_t)(((nk - 1) >> 1) & 1), timeout_ns);
     ok = __syncthreads_and(ok) != 0;
@@ -360,8 +362,12 @@ __global__ void __launch_bounds__(TC_THREADS) k_gemm_tc(GemmArgs g, long long ti
                 }
             }
         }
-    } else if (threadIdx.x == 0) {
-        atomicExch(&g_tc_err, 1);
+    } else {
+        if (threadIdx.x == 0) atomicExch(&g_tc_err, 1);
+        // a wait ran out: give the MMAs already committed (the last commit
+        // covers every earlier one) one more bounded wait before the
+        // accumulator's tensor memory is freed
+        if (issued > 0) mbar_wait(&bar[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), timeout_ns);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -560,7 +566,13 @@ __global__ void __launch_bounds__(TC_THREADS) k_mlp_fwd(MlpArgs a, long long tim
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         }
     }
-    if (!ok && threadIdx.x == 0) atomicExch(&g_tc_err, 1);
+    if (!ok) {
+        if (threadIdx.x == 0) atomicExch(&g_tc_err, 1);
+        // g K chunks were committed (a chunk counts once its MMAs are
+        // issued): one more bounded wait on the last commit before the
+        // tensor memory is freed
+        if (g > 0) mbar_wait(&bar[(g - 1) & 1], (uint32_t)(((g - 1) >> 1) & 1), timeout_ns);
+    }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0)
